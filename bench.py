@@ -1,0 +1,373 @@
+"""Throughput of the fused lattice Boltzmann step on GB300.
+
+Workload (default): D3Q19 BGK lid-driven cavity, 512^3 cells, FP32FP32 policy,
+FullwayBounceBack on five faces, EquilibriumBC lid u = (0.05, 0, 0) on the
+z = 511 face without edges, omega = 1.8, rest equilibrium start.  One "step" is
+one fused time step over all 134.2 M cells.  Metric: MLUPS (all cells, as
+XLB's examples/performance/mlups_3d.py:87-90 counts them).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  The population fields (2 x 10.7 GB) are far larger than
+L2, so no L2 flush is needed between steps.  Under torchrun with N > 1 every
+rank runs the same workload on its own GPU (independent replicas, the path has
+no cross-GPU step here) and the value is the sum over ranks measured against
+the slowest rank.
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "D3Q19 MLUPS"
+BYTES_PER_CELL = {("D3Q19", 4): 153, ("D3Q19", 2): 77, ("D3Q19", 8): 305, ("D2Q9", 4): 73, ("D3Q27", 4): 217}
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=1000)
+    p.add_argument("--warmup", type=int, default=100)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--n", type=int, default=512, help="cube edge")
+    p.add_argument("--no-forms", action="store_true", help="skip the FP16/BF16 store-form lines")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled while the timed region runs."""
+
+    FIELDS = "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True,
+            )
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cavity_setup(n, policy_name, omega=1.8):
+    """The cavity: stepper and prepared fields on the current device."""
+    import numpy as np
+
+    import xlb_gb300 as xlb
+    from xlb_gb300.operator.boundary_condition import EquilibriumBC, FullwayBounceBackBC
+    from xlb_gb300.operator.stepper import IncompressibleNavierStokesStepper
+
+    pp = getattr(xlb.PrecisionPolicy, policy_name)
+    xlb.init(xlb.velocity_set.D3Q19(pp), xlb.ComputeBackend.CUDA, pp)
+    grid = xlb.grid.grid_factory((n, n, n))
+    box = grid.bounding_box_indices()
+    nob = grid.bounding_box_indices(remove_edges=True)
+    walls = [box["bottom"][i] + box["left"][i] + box["right"][i] + box["front"][i] + box["back"][i] for i in range(3)]
+    walls = np.unique(np.array(walls), axis=-1).tolist()
+    bcs = [EquilibriumBC(rho=1.0, u=(0.05, 0.0, 0.0), indices=nob["top"]), FullwayBounceBackBC(indices=walls)]
+    stepper = IncompressibleNavierStokesStepper(grid, bcs, collision_type="BGK")
+    fields = stepper.prepare_fields()
+    return stepper, fields, omega
+
+
+def timed_device(stepper, fields, omega, steps, warmup):
+    """W untimed steps, then K steps bracketed by synchronize + CUDA events on the launching stream."""
+    import torch
+
+    f_0, f_1, bcm, mm = fields
+    f_0, f_1 = stepper.run(f_0, f_1, bcm, mm, omega, warmup)
+    torch.cuda.synchronize()
+    barrier()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record()
+    f_0, f_1 = stepper.run(f_0, f_1, bcm, mm, omega, steps, timestep0=warmup)
+    end.record()
+    torch.cuda.synchronize()
+    return start.elapsed_time(end), (f_0, f_1, bcm, mm)
+
+
+def timed_e2e(stepper, fields, omega, steps):
+    """The job through the public API with host buffers: H2D of the initial
+    populations and masks from pinned host memory, K per-step ``stepper(...)``
+    calls with the caller-side swap, D2H of the final populations."""
+    import torch
+
+    f_0, f_1, bcm, mm = fields
+    hf = torch.empty(f_0.shape, dtype=f_0.dtype, pin_memory=True)
+    hf.copy_(f_0)
+    hb = bcm.cpu().pin_memory()
+    hm = mm.cpu().pin_memory()
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    f_0.copy_(hf, non_blocking=True)
+    f_1.copy_(hf, non_blocking=True)
+    bcm.copy_(hb, non_blocking=True)
+    mm.copy_(hm, non_blocking=True)
+    for i in range(steps):
+        f_0, f_1 = stepper(f_0, f_1, bcm, mm, omega, i)
+        f_0, f_1 = f_1, f_0
+    hf.copy_(f_0, non_blocking=True)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    h2d = 2 * hf.numel() * hf.element_size() + hb.numel() + hm.numel()
+    d2h = hf.numel() * hf.element_size()
+    return dt, h2d, d2h
+
+
+_dist = None
+
+
+def barrier():
+    if _dist is not None:
+        _dist.barrier()
+
+
+def max_over_ranks(x):
+    if _dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    _dist.all_reduce(t, op=_dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_baseline_sample(n=32, steps=2):
+    """The CPU restatement of the step timed on this host, on a D3Q19 cavity sample."""
+    import numpy as np
+
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle import lbm_oracle as O
+
+    lat = O.Lattice("D3Q19")
+    st = O.Store("f32", lat)
+    shape = (n, n, n)
+    from xlb_gb300.grid import grid_factory
+
+    g = grid_factory(shape, device="cpu")
+    box, nob = g.bounding_box_indices(), g.bounding_box_indices(remove_edges=True)
+    walls = np.unique(np.array([box["bottom"][i] + box["left"][i] + box["right"][i] + box["front"][i] + box["back"][i] for i in range(3)]), axis=-1)
+    bcs = [O.BC("equilibrium", 1, nob["top"], rho=1.0, u=(0.05, 0.0, 0.0)), O.BC("fullway_bb", 2, walls)]
+    bcm, miss = O.masker(lat, shape, bcs)
+    f0 = O.initial_equilibrium(lat, st, shape, np.float32)
+    f1 = f0.copy()
+    t0 = time.perf_counter()
+    O.run(lat, st, f0, f1, bcm, miss, 1.8, bcs, steps, "BGK", np.float32)
+    dt = time.perf_counter() - t0
+    return {
+        "value": n**3 * steps / dt / 1e6,
+        "unit": "MLUPS",
+        "cores": 1,
+        "kind": "port",
+        "sample": f"numpy float32 restatement of the fused step, D3Q19 BGK cavity {n}^3, {steps} steps",
+    }
+
+
+def run_reference(args):
+    """--impl reference: the CPU implementation of the path (the restatement; XLB itself
+    needs warp/jax, which are not installable here) on this host's cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import numpy as np
+
+    from oracle import lbm_oracle as O
+    from xlb_gb300.grid import grid_factory
+
+    n = 32
+    lat = O.Lattice("D3Q19")
+    st = O.Store("f32", lat)
+    shape = (n, n, n)
+    g = grid_factory(shape, device="cpu")
+    box, nob = g.bounding_box_indices(), g.bounding_box_indices(remove_edges=True)
+    walls = np.unique(np.array([box["bottom"][i] + box["left"][i] + box["right"][i] + box["front"][i] + box["back"][i] for i in range(3)]), axis=-1)
+    bcs = [O.BC("equilibrium", 1, nob["top"], rho=1.0, u=(0.05, 0.0, 0.0)), O.BC("fullway_bb", 2, walls)]
+    bcm, miss = O.masker(lat, shape, bcs)
+    f0 = O.initial_equilibrium(lat, st, shape, np.float32)
+    f1 = f0.copy()
+    f0, f1 = O.run(lat, st, f0, f1, bcm, miss, 1.8, bcs, args.warmup, "BGK", np.float32)
+    t0 = time.perf_counter()
+    O.run(lat, st, f0, f1, bcm, miss, 1.8, bcs, args.steps, "BGK", np.float32)
+    dt = time.perf_counter() - t0
+    v = n**3 * args.steps / dt / 1e6
+    sample = f"numpy float32 restatement, D3Q19 BGK cavity {n}^3 per step (sample of the 512^3 workload)"
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "MLUPS", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dt * 1e3 / max(1, args.steps), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"D3Q19 BGK lid-driven cavity {n}^3 sample of 512^3, FP32FP32", "cells": n**3},
+        "cpu_baseline": {"value": v, "unit": "MLUPS", "cores": 1, "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def main():
+    global _dist
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+        _dist = dist
+
+    from xlb_gb300 import _lib
+
+    _lib.load()
+    n = args.n
+    cells = n**3
+    peak, peak_kind = measured_peaks()
+
+    stepper, fields, omega = cavity_setup(n, "FP32FP32")
+    with ClockSampler(local) as clk:
+        ms, fields = timed_device(stepper, fields, omega, args.steps, args.warmup)
+    ms = max_over_ranks(ms)
+    mlups = world * cells * args.steps / (ms * 1e-3) / 1e6
+    per_launch_s = ms * 1e-3 / args.steps
+    bpc = BYTES_PER_CELL[("D3Q19", 4)]
+    achieved = bpc * cells / per_launch_s / 1e9
+    out = {
+        "metric": METRIC,
+        "value": mlups,
+        "unit": "MLUPS",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {
+            "workload": f"D3Q19 BGK lid-driven cavity {n}^3, FP32FP32, FullwayBB x5 faces + EquilibriumBC lid u=(0.05,0,0), omega=1.8",
+            "cells": cells,
+            "l2": "inputs (2 x %.1f GB populations) larger than L2; no flush" % (cells * 19 * 4 / 1e9),
+            "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+        },
+        "gpu_launches": args.steps,
+        "roofline": {
+            "bound": "hbm",
+            "achieved": achieved,
+            "peak": peak,
+            "unit": "GB/s",
+            "frac": achieved / peak,
+            "traffic": load_traffic(n),
+            "bytes_per_cell": bpc,
+            "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})",
+        },
+        "clocks": clk.summary(),
+    }
+    if not args.no_forms:
+        forms = {}
+        del fields, stepper
+        torch.cuda.empty_cache()
+        for name, pol in (("fp16_shifted", "FP32FP16S"), ("bf16_shifted", "FP32BF16S")):
+            st, fl, om = cavity_setup(n, pol)
+            ms2, fl = timed_device(st, fl, om, args.steps, args.warmup)
+            ms2 = max_over_ranks(ms2)
+            v = world * cells * args.steps / (ms2 * 1e-3) / 1e6
+            ach = BYTES_PER_CELL[("D3Q19", 2)] * cells / (ms2 * 1e-3 / args.steps) / 1e9
+            forms[name] = {"MLUPS": v, "x_fp32": v / mlups, "achieved_GBs": ach, "frac": ach / peak, "bytes_per_cell": 77}
+            del st, fl
+            torch.cuda.empty_cache()
+        out["store_forms"] = forms
+        stepper, fields, omega = cavity_setup(n, "FP32FP32")
+    if not args.no_e2e:
+        dt, h2d, d2h = timed_e2e(stepper, fields, omega, args.steps)
+        dt = max_over_ranks(dt)
+        out["e2e"] = {
+            "value": world * cells * args.steps / dt / 1e6,
+            "unit": "MLUPS",
+            "h2d_bytes_per_step": h2d / args.steps,
+            "d2h_bytes_per_step": d2h / args.steps,
+            "what": "public stepper(...) call per step with caller swap; initial populations+masks H2D from pinned host and final populations D2H inside the timed region",
+        }
+    if not args.no_cpu and rank == 0:
+        out["cpu_baseline"] = cpu_baseline_sample()
+    if rank == 0:
+        print(json.dumps(out))
+    if _dist is not None:
+        _dist.destroy_process_group()
+
+
+def load_traffic(n):
+    """dram bytes per launch from the committed ncu summary of this kernel, when present."""
+    path = os.path.join(ROOT, "profiles", "step_d3q19_cavity_traffic.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as fh:
+        d = json.load(fh)
+    # traffic grows with the cell count; scale from the captured case
+    return d["dram_bytes_per_launch"] * (n**3) / d["cells"]
+
+
+if __name__ == "__main__":
+    main()

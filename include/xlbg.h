@@ -1,0 +1,164 @@
+/*
+ * xlbg.h -- C ABI of the GB300 lattice Boltzmann time-step library (libxlbg.so).
+ *
+ * Every entry point takes plain device pointers, sizes and a CUDA stream
+ * (cudaStream_t passed as void*), returns an int status (XLBG_OK == 0) and
+ * never allocates device memory.  Launches are asynchronous on the given
+ * stream; nothing synchronises.  The last error message of the calling thread
+ * is available from xlbg_last_error().
+ *
+ * Field layout is XLB's Warp layout (xlb/grid/warp_grid.py:17-32): a population
+ * field is (Q, nx, ny, nz) C-contiguous with nz fastest; 2D fields are
+ * (Q, nx, ny, 1).  bc_mask is (1, nx, ny, nz) uint8 (0 fluid, 255 skipped).
+ *
+ * Each declaration names the XLB interface it replaces (file:line in the XLB
+ * source tree).
+ */
+#ifndef XLBG_H
+#define XLBG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define XLBG_ABI_VERSION 1
+#define XLBG_MAX_BC 16
+#define XLBG_DIAG_SLOTS 1024
+
+/* status codes */
+enum {
+  XLBG_OK = 0,
+  XLBG_ERR_ARG = 1,         /* null pointer, bad size or out-of-range enum */
+  XLBG_ERR_UNSUPPORTED = 2, /* e.g. KBC with D3Q19, shifted store with FP64 compute */
+  XLBG_ERR_ALIGN = 3,       /* pointer not aligned to its element size */
+  XLBG_ERR_CUDA = 4         /* a CUDA launch or API call failed */
+};
+
+/* lattice (xlb/velocity_set/{d2q9,d3q19,d3q27}.py) */
+enum { XLBG_D2Q9 = 0, XLBG_D3Q19 = 1, XLBG_D3Q27 = 2 };
+
+/* store form of populations (xlb/precision_policy.py:46-81, plus shifted forms) */
+enum {
+  XLBG_STORE_F32 = 0,
+  XLBG_STORE_F64 = 1,
+  XLBG_STORE_F16 = 2,   /* raw FP16, XLB's FP32FP16 / FP64FP16 */
+  XLBG_STORE_F16S = 3,  /* FP16 holding f - w_l */
+  XLBG_STORE_BF16S = 4  /* BF16 holding f - w_l */
+};
+enum { XLBG_COMPUTE_F32 = 0, XLBG_COMPUTE_F64 = 1 };
+
+/* collision (xlb/operator/collision/bgk.py:30-34, kbc.py:192-296) */
+enum { XLBG_BGK = 0, XLBG_KBC = 1 };
+
+/* boundary-condition kinds (xlb/operator/boundary_condition/bc_*.py) */
+enum {
+  XLBG_BC_FULLWAY_BB = 1,            /* bc_fullway_bounce_back.py:59-72 */
+  XLBG_BC_HALFWAY_BB = 2,            /* bc_halfway_bounce_back.py:67-85 */
+  XLBG_BC_EQUILIBRIUM = 3,           /* bc_equilibrium.py:75-86 */
+  XLBG_BC_ZOUHE_VELOCITY = 4,        /* bc_zouhe.py:279-313 */
+  XLBG_BC_ZOUHE_PRESSURE = 5,        /* bc_zouhe.py:315-343 */
+  XLBG_BC_REGULARIZED_VELOCITY = 6,  /* bc_regularized.py:134-169 */
+  XLBG_BC_REGULARIZED_PRESSURE = 7,  /* bc_regularized.py:171-202 */
+  XLBG_BC_EXTRAPOLATION = 8          /* bc_extrapolation_outflow.py:372-415 */
+};
+
+typedef struct {
+  int32_t id;     /* uint8 id written into bc_mask, 1..254 */
+  int32_t kind;   /* XLBG_BC_* */
+  double rho;     /* EquilibriumBC density */
+  double u[3];    /* EquilibriumBC velocity (u[2] unused in 2D) */
+} xlbg_bc;
+
+/*
+ * Static description of a stepper.  Replaces the objects XLB bakes into its
+ * Warp kernel at construction (nse_stepper.py:25-56, 245-263): velocity set,
+ * precision policy, collision type, grid shape and the BC list.
+ */
+typedef struct {
+  int32_t abi_version; /* XLBG_ABI_VERSION */
+  int32_t lattice;     /* XLBG_D2Q9 / XLBG_D3Q19 / XLBG_D3Q27 */
+  int32_t store;       /* XLBG_STORE_* */
+  int32_t compute;     /* XLBG_COMPUTE_* */
+  int32_t collision;   /* XLBG_BGK / XLBG_KBC */
+  int32_t nbc;         /* entries used in bc[] */
+  int64_t nx, ny, nz;  /* grid shape; nz = 1 for 2D */
+  xlbg_bc bc[XLBG_MAX_BC];
+} xlbg_desc;
+
+/* Library and lattice introspection (host only, no GPU needed). */
+int xlbg_abi_version(void);
+const char* xlbg_last_error(void);
+/* c: q*d int32 (c[l*d + k]), w: q doubles, opp: q int32.  Returns q, or <0. */
+int xlbg_lattice_tables(int32_t lattice, int32_t* c, double* w, int32_t* opp);
+
+/*
+ * Pack XLB's bool missing_mask (Q, nx, ny, nz) into one uint32 per cell, bit l
+ * set when direction l is missing.  Replaces the per-step Q-byte read of the
+ * mask in nse_stepper.py:311; called once at set-up.
+ */
+int xlbg_pack_missing(const xlbg_desc* desc, const uint8_t* missing_mask, uint32_t* miss_bits, void* stream);
+
+/*
+ * One fused time step: pull stream, streaming-step BCs, macroscopic, quadratic
+ * equilibrium, collision, collision-step BCs, extrapolation aux data, aux
+ * recovery into f0, store into f1.  Replaces
+ * IncompressibleNavierStokesStepper.warp_implementation (nse_stepper.py:385-392)
+ * and its kernel (:344-382).  omega is the relaxation rate, timestep is kept for
+ * signature parity (unused by the built-in BCs, as in XLB).
+ *
+ * rec_cells/n_rec: linear indices of the cells whose bc id is a ZouHe or
+ * Regularized BC (sorted, int64); rec_scratch: n_rec*Q elements of the store
+ * type.  Both may be NULL/0 when the BC list has no such BC.  The recovery
+ * writes into f0 happen after every pull of the step, which makes the step
+ * deterministic where XLB's kernel races (nse_stepper.py:338-342).
+ */
+int xlbg_step(const xlbg_desc* desc, void* f0, void* f1, const uint8_t* bc_mask, const uint32_t* miss_bits,
+              const int64_t* rec_cells, int64_t n_rec, void* rec_scratch, double omega, int32_t timestep,
+              void* stream);
+
+/*
+ * n_steps steps with the caller-side swap of XLB's examples
+ * (examples/performance/mlups_3d.py:78-80) done inside: step k reads the
+ * buffer written by step k-1.  After an odd n_steps the newest state is in
+ * f1, after an even n_steps it is in f0.
+ */
+int xlbg_run(const xlbg_desc* desc, void* f0, void* f1, const uint8_t* bc_mask, const uint32_t* miss_bits,
+             const int64_t* rec_cells, int64_t n_rec, void* rec_scratch, double omega, int32_t timestep0,
+             int32_t n_steps, void* stream);
+
+/*
+ * A step that also returns diagnostics of the states it touches, in FP64:
+ *   diag[0] = total mass of the OUTPUT state (sum over non-skipped cells of
+ *             sum_l f1_l as stored),
+ *   diag[1..d] = momentum-exchange force on the no-slip BC with id force_id
+ *             evaluated on the INPUT state f0 -- the value XLB's
+ *             MomentumTransfer (xlb/operator/force/momentum_transfer.py:92-176)
+ *             returns when called on f0 after the previous step's swap.
+ * force_id < 0 disables the force.  diag_slots is caller scratch of
+ * XLBG_DIAG_SLOTS*4 doubles that must be zero on entry and is left zero.
+ */
+int xlbg_step_diag(const xlbg_desc* desc, void* f0, void* f1, const uint8_t* bc_mask, const uint32_t* miss_bits,
+                   const int64_t* rec_cells, int64_t n_rec, void* rec_scratch, double omega, int32_t timestep,
+                   int32_t force_id, double* diag_slots, double* diag, void* stream);
+
+/*
+ * f = feq(rho, u) in the store form for every cell (initializers.py:5-20 with
+ * quadratic_equilibrium.py:63-82).  rho: (1, cells) and u: (d, cells) in the
+ * compute type, or NULL for the uniform values rho0 / u0[d].
+ */
+int xlbg_equilibrium(const xlbg_desc* desc, const void* rho, const void* u, double rho0, const double* u0, void* f,
+                     void* stream);
+
+/*
+ * rho (1, cells) and u (d, cells) in the compute type from a population field
+ * (xlb/operator/macroscopic/macroscopic.py:39-55).
+ */
+int xlbg_macroscopic(const xlbg_desc* desc, const void* f, void* rho, void* u, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* XLBG_H */

@@ -1,0 +1,90 @@
+"""libxlbg.so loads, exports every entry point include/xlbg.h declares, and
+rejects bad descriptors on the host (no GPU work is launched by these calls)."""
+
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import xlb_gb300 as xlb
+from xlb_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if fn.endswith(".h"):
+            src = open(os.path.join(ROOT, "include", fn)).read()
+            names |= set(re.findall(r"^\s*(?:const\s+)?\w+\**\s+\**(xlbg_\w+)\s*\(", src, flags=re.M))
+    return sorted(names)
+
+
+def test_library_loads_and_exports_every_declared_symbol():
+    lib = _lib.load()
+    names = declared_symbols()
+    assert len(names) >= 9
+    for n in names:
+        assert hasattr(lib, n), n
+    assert set(_lib.EXPORTED) <= set(names)
+    assert lib.xlbg_abi_version() == _lib.ABI_VERSION
+
+
+@pytest.mark.parametrize("code,cls", [(0, xlb.velocity_set.D2Q9), (1, xlb.velocity_set.D3Q19), (2, xlb.velocity_set.D3Q27)])
+def test_compiled_lattice_tables_match_velocity_sets(code, cls):
+    vs = cls()
+    c, w, opp = _lib.lattice_tables(code)
+    assert np.array_equal(c.T, vs.c)
+    assert np.array_equal(w, vs.w)  # bit-identical doubles
+    assert np.array_equal(opp, vs.opp_indices)
+
+
+def _desc(**kw):
+    d = _lib.Desc()
+    d.abi_version = _lib.ABI_VERSION
+    d.lattice, d.store, d.compute, d.collision, d.nbc = 1, 0, 0, 0, 0
+    d.nx = d.ny = d.nz = 8
+    for k, v in kw.items():
+        setattr(d, k, v)
+    return d
+
+
+def _step(desc, f0=1024, f1=2048):
+    lib = _lib.load()
+    p = ctypes.c_void_p
+    return lib.xlbg_step(desc, p(f0), p(f1), p(4096), p(8192), None, 0, None, 1.0, 0, None)
+
+
+def test_null_and_bad_descriptors_are_rejected():
+    lib = _lib.load()
+    p = ctypes.c_void_p
+    assert lib.xlbg_step(None, p(16), p(32), p(64), p(128), None, 0, None, 1.0, 0, None) == _lib.ERR_ARG
+    assert b"NULL" in lib.xlbg_last_error()
+    assert _step(_desc(abi_version=99)) == _lib.ERR_ARG
+    assert _step(_desc(lattice=7)) == _lib.ERR_ARG
+    assert _step(_desc(collision=_lib.KBC)) == _lib.ERR_UNSUPPORTED
+    assert b"D2Q9 and D3Q27" in lib.xlbg_last_error()
+    assert _step(_desc(compute=1, store=3)) == _lib.ERR_UNSUPPORTED
+    assert _step(_desc(lattice=0, nz=4)) == _lib.ERR_ARG
+    assert _step(_desc(nx=0)) == _lib.ERR_ARG
+    d = _desc(nbc=1)
+    d.bc[0].id, d.bc[0].kind = 255, _lib.BC_FULLWAY_BB
+    assert _step(d) == _lib.ERR_ARG
+
+
+def test_pointer_checks():
+    assert _step(_desc(), f0=1026) == _lib.ERR_ALIGN
+    assert _step(_desc(), f0=1024, f1=1024) == _lib.ERR_ARG
+    lib = _lib.load()
+    p = ctypes.c_void_p
+    # n_rec > 0 needs both the cell list and the scratch
+    assert lib.xlbg_step(_desc(), p(1024), p(2048), p(4096), p(8192), None, 5, None, 1.0, 0, None) == _lib.ERR_ARG
+
+
+def test_xlbg_error_carries_message():
+    with pytest.raises(_lib.XlbgError) as e:
+        _lib.check(_step(_desc(collision=_lib.KBC)))
+    assert e.value.code == _lib.ERR_UNSUPPORTED

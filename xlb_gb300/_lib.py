@@ -1,0 +1,150 @@
+"""ctypes binding of libxlbg.so (the C ABI declared in include/xlbg.h).
+
+The library is loaded from ``xlb_gb300/lib/libxlbg.so`` (built in-tree by
+``xlb_gb300/build.py``).  There is no fallback: if the library is missing or a
+call fails, an exception is raised.
+"""
+
+import ctypes
+import os
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libxlbg.so")
+
+ABI_VERSION = 1
+MAX_BC = 16
+DIAG_SLOTS = 1024
+
+OK, ERR_ARG, ERR_UNSUPPORTED, ERR_ALIGN, ERR_CUDA = 0, 1, 2, 3, 4
+
+BC_FULLWAY_BB = 1
+BC_HALFWAY_BB = 2
+BC_EQUILIBRIUM = 3
+BC_ZOUHE_VELOCITY = 4
+BC_ZOUHE_PRESSURE = 5
+BC_REGULARIZED_VELOCITY = 6
+BC_REGULARIZED_PRESSURE = 7
+BC_EXTRAPOLATION = 8
+
+BGK, KBC = 0, 1
+
+EXPORTED = (
+    "xlbg_abi_version",
+    "xlbg_last_error",
+    "xlbg_lattice_tables",
+    "xlbg_pack_missing",
+    "xlbg_step",
+    "xlbg_run",
+    "xlbg_step_diag",
+    "xlbg_equilibrium",
+    "xlbg_macroscopic",
+)
+
+
+class XlbgError(RuntimeError):
+    """A C-ABI call returned a non-zero status."""
+
+    def __init__(self, code, msg):
+        super().__init__(f"xlbg error {code}: {msg}")
+        self.code = code
+
+
+class BCEntry(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_int32), ("kind", ctypes.c_int32), ("rho", ctypes.c_double), ("u", ctypes.c_double * 3)]
+
+
+class Desc(ctypes.Structure):
+    _fields_ = [
+        ("abi_version", ctypes.c_int32),
+        ("lattice", ctypes.c_int32),
+        ("store", ctypes.c_int32),
+        ("compute", ctypes.c_int32),
+        ("collision", ctypes.c_int32),
+        ("nbc", ctypes.c_int32),
+        ("nx", ctypes.c_int64),
+        ("ny", ctypes.c_int64),
+        ("nz", ctypes.c_int64),
+        ("bc", BCEntry * MAX_BC),
+    ]
+
+
+_lock = threading.Lock()
+_lib = None
+
+_P = ctypes.c_void_p
+_I32 = ctypes.c_int32
+_I64 = ctypes.c_int64
+_D = ctypes.c_double
+_DESC = ctypes.POINTER(Desc)
+
+_SIGNATURES = {
+    "xlbg_abi_version": ([], ctypes.c_int),
+    "xlbg_last_error": ([], ctypes.c_char_p),
+    "xlbg_lattice_tables": ([_I32, ctypes.POINTER(_I32), ctypes.POINTER(_D), ctypes.POINTER(_I32)], ctypes.c_int),
+    "xlbg_pack_missing": ([_DESC, _P, _P, _P], ctypes.c_int),
+    "xlbg_step": ([_DESC, _P, _P, _P, _P, _P, _I64, _P, _D, _I32, _P], ctypes.c_int),
+    "xlbg_run": ([_DESC, _P, _P, _P, _P, _P, _I64, _P, _D, _I32, _I32, _P], ctypes.c_int),
+    "xlbg_step_diag": ([_DESC, _P, _P, _P, _P, _P, _I64, _P, _D, _I32, _I32, _P, _P, _P], ctypes.c_int),
+    "xlbg_equilibrium": ([_DESC, _P, _P, _D, ctypes.POINTER(_D), _P, _P], ctypes.c_int),
+    "xlbg_macroscopic": ([_DESC, _P, _P, _P, _P], ctypes.c_int),
+}
+
+
+def load(build_if_missing=True):
+    """Load libxlbg.so (building it first when absent and nvcc is available)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH) and build_if_missing:
+            from xlb_gb300 import build as _build
+
+            _build.build()
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"libxlbg.so not found at {LIB_PATH}; run xlb_gb300/build.py")
+        lib = ctypes.CDLL(LIB_PATH)
+        for name, (args, res) in _SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.argtypes = args
+            fn.restype = res
+        if lib.xlbg_abi_version() != ABI_VERSION:
+            raise ImportError("libxlbg.so ABI version mismatch; rebuild it")
+        _lib = lib
+        return lib
+
+
+def check(status):
+    if status != OK:
+        msg = load().xlbg_last_error().decode(errors="replace")
+        raise XlbgError(status, msg)
+
+
+def lattice_tables(lattice):
+    """(c (q, d), w (q,), opp (q,)) as compiled into the kernels."""
+    import numpy as np
+
+    c = (_I32 * (27 * 3))()
+    w = (_D * 27)()
+    o = (_I32 * 27)()
+    q = load().xlbg_lattice_tables(lattice, c, w, o)
+    if q < 0:
+        check(-q)
+    d = 2 if lattice == 0 else 3
+    return (
+        np.array(c[: q * d], dtype=np.int64).reshape(q, d),
+        np.array(w[:q], dtype=np.float64),
+        np.array(o[:q], dtype=np.int64),
+    )
+
+
+def ptr(t):
+    """Device pointer of a torch tensor, or None."""
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def stream_handle(stream=None):
+    import torch
+
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)

@@ -1,0 +1,205 @@
+// Per-cell physics: moments, equilibrium, BGK, KBC and the boundary functionals.
+//
+// Each function keeps the operation order of the XLB functional it replaces so
+// that, built with --fmad=false, results match the CPU oracle bit for bit.
+#pragma once
+#include "lattice.cuh"
+
+namespace xlbg {
+
+// rho = sum_l f_l ; u_d = (sum_{c_dl=+1} f_l - sum_{c_dl=-1} f_l) / rho
+// (zero_moment.py:137-141, first_moment.py:188-201)
+template <class L, class T>
+__device__ __forceinline__ void macroscopic(const T (&f)[L::Q], T& rho, T (&u)[L::D]) {
+  rho = T(0) + f[0];
+#pragma unroll
+  for (int l = 1; l < L::Q; ++l) rho = rho + f[l];
+#pragma unroll
+  for (int d = 0; d < L::D; ++d) {
+    T acc = T(0);
+#pragma unroll
+    for (int l = 0; l < L::Q; ++l) {
+      if (L::c(l, d) == 1) acc = acc + f[l];
+      if (L::c(l, d) == -1) acc = acc - f[l];
+    }
+    u[d] = acc / rho;
+  }
+}
+
+// feq_l = rho w_l (1 + cu (1 + cu/2) - 1.5 |u|^2), cu = 3 c_l.u (quadratic_equilibrium.py:331-356)
+template <class L, class T>
+__device__ __forceinline__ T feq_l(int l, T rho, const T (&u)[L::D], T usqr) {
+  T cu = T(0);
+#pragma unroll
+  for (int d = 0; d < L::D; ++d) {
+    if (L::c(l, d) == 1) cu = cu + u[d];
+    if (L::c(l, d) == -1) cu = cu - u[d];
+  }
+  cu = cu * T(3);
+  return rho * T(weight<L>(l)) * (T(1) + cu * (T(1) + T(0.5) * cu) - usqr);
+}
+
+template <class L, class T>
+__device__ __forceinline__ T usqr_of(const T (&u)[L::D]) {
+  T s = u[0] * u[0];
+#pragma unroll
+  for (int d = 1; d < L::D; ++d) s = s + u[d] * u[d];
+  return T(1.5) * s;
+}
+
+template <class L, class T>
+__device__ __forceinline__ void equilibrium(T rho, const T (&u)[L::D], T (&feq)[L::Q]) {
+  const T usqr = usqr_of<L>(u);
+#pragma unroll
+  for (int l = 0; l < L::Q; ++l) feq[l] = feq_l<L>(l, rho, u, usqr);
+}
+
+// Pi_t = sum_q cc_qt fneq_q, with cc in {-1, 0, 1} (second_moment.py:416-426)
+template <class L, class T>
+__device__ __forceinline__ void second_moment(const T (&fneq)[L::Q], T (&pi)[L::NT]) {
+#pragma unroll
+  for (int t = 0; t < L::NT; ++t) {
+    T acc = T(0);
+#pragma unroll
+    for (int q = 0; q < L::Q; ++q) {
+      if (cc<L>(q, t) == 1) acc = acc + fneq[q];
+      if (cc<L>(q, t) == -1) acc = acc - fneq[q];
+    }
+    pi[t] = acc;
+  }
+}
+
+// Entropic KBC (kbc.py:192-296); defined for D2Q9 and D3Q27 only.
+template <class L, class T>
+__device__ __forceinline__ void kbc(const T (&f)[L::Q], const T (&feq)[L::Q], T rho, T omega, T (&fo)[L::Q]) {
+  T fneq[L::Q];
+#pragma unroll
+  for (int l = 0; l < L::Q; ++l) fneq[l] = f[l] - feq[l];
+  T pi[L::NT];
+  second_moment<L>(fneq, pi);
+  T ds[L::Q];
+#pragma unroll
+  for (int l = 0; l < L::Q; ++l) ds[l] = T(0);
+  const T two = T(2), four = T(4), six = T(6);
+  if constexpr (L::Q == 27) {
+    const T nxz = pi[0] - pi[5];
+    const T nyz = pi[3] - pi[5];
+    const T a = (two * nxz - nyz) / six;
+    const T b = (-nxz + two * nyz) / six;
+    const T cz = (-nxz - nyz) / six;
+    const T p1 = pi[1] / four, p2 = pi[2] / four, p4 = pi[4] / four;
+    const T m1 = -pi[1] / four, m2 = -pi[2] / four, m4 = -pi[4] / four;
+    ds[9] = a; ds[18] = a; ds[3] = b; ds[6] = b; ds[1] = cz; ds[2] = cz;
+    ds[12] = p1; ds[24] = p1; ds[21] = m1; ds[15] = m1;
+    ds[10] = p2; ds[20] = p2; ds[19] = m2; ds[11] = m2;
+    ds[8] = p4; ds[4] = p4; ds[7] = m4; ds[5] = m4;
+#pragma unroll
+    for (int l = 0; l < L::Q; ++l) ds[l] = ds[l] * rho;
+  } else {
+    const T n = pi[0] - pi[2];
+    ds[3] = n; ds[6] = n; ds[2] = -n; ds[1] = -n;
+    ds[8] = pi[1]; ds[4] = -pi[1]; ds[5] = -pi[1]; ds[7] = pi[1];
+#pragma unroll
+    for (int l = 0; l < L::Q; ++l) ds[l] = ds[l] * rho / four;
+  }
+  const T beta = T(0.5) * omega;
+  const T inv_beta = T(1) / beta;
+  T dh[L::Q];
+  T sp1 = T(0), sp2 = T(0);
+#pragma unroll
+  for (int l = 0; l < L::Q; ++l) {
+    dh[l] = fneq[l] - ds[l];
+    const T temp = dh[l] / feq[l];
+    sp1 = sp1 + temp * ds[l];
+    sp2 = sp2 + temp * dh[l];
+  }
+  const T gamma = inv_beta - (two - inv_beta) * sp1 / (T(1e-32) + sp2);
+#pragma unroll
+  for (int l = 0; l < L::Q; ++l) fo[l] = f[l] - beta * (two * ds[l] + gamma * dh[l]);
+}
+
+// -c of the first missing direction with |c|_1 = 1 (helper_functions_bc.py:250-261,
+// bc_extrapolation_outflow.py:358-369).  Zero when there is none.
+template <class L>
+__device__ __forceinline__ void normal_of(uint32_t miss, int (&nv)[L::D]) {
+  bool found = false;
+#pragma unroll
+  for (int d = 0; d < L::D; ++d) nv[d] = 0;
+#pragma unroll
+  for (int l = 0; l < L::Q; ++l) {
+    if (norm1<L>(l) == 1) {
+      if (!found && ((miss >> l) & 1u)) {
+        found = true;
+#pragma unroll
+        for (int d = 0; d < L::D; ++d) nv[d] = -L::c(l, d);
+      }
+    }
+  }
+}
+
+// BC kinds (include/xlbg.h)
+enum {
+  BC_FULLWAY = 1,
+  BC_HALFWAY = 2,
+  BC_EQUILIBRIUM = 3,
+  BC_ZOUHE_V = 4,
+  BC_ZOUHE_P = 5,
+  BC_REG_V = 6,
+  BC_REG_P = 7,
+  BC_EXTRAP = 8
+};
+
+// ZouHe and Regularized, velocity or pressure (bc_zouhe.py:279-343,
+// bc_regularized.py:134-202, helpers helper_functions_bc.py:236-297).
+template <class L, class T>
+__device__ __forceinline__ void zouhe_like(T (&f)[L::Q], uint32_t miss, T aux, int kind) {
+  int nv[L::D];
+  normal_of<L>(miss, nv);
+  T known = T(0), middle = T(0);
+#pragma unroll
+  for (int l = 0; l < L::Q; ++l) {
+    const bool k = (miss >> opp<L>(l)) & 1u;
+    const bool m = !k && !((miss >> l) & 1u);
+    if (k) known = known + T(2) * f[l];
+    if (m) middle = middle + f[l];
+  }
+  const T fsum = known + middle;
+  T rho, u[L::D];
+  if (kind == BC_ZOUHE_V || kind == BC_REG_V) {
+    T unormal = T(0);
+#pragma unroll
+    for (int d = 0; d < L::D; ++d) u[d] = (-aux) * T(nv[d]);
+#pragma unroll
+    for (int d = 0; d < L::D; ++d) unormal = unormal + u[d] * T(nv[d]);
+    rho = fsum / (T(1) + unormal);
+  } else {
+    rho = aux;
+    const T unormal = T(-1) + fsum / rho;
+#pragma unroll
+    for (int d = 0; d < L::D; ++d) u[d] = unormal * T(nv[d]);
+  }
+  T feq[L::Q];
+  equilibrium<L>(rho, u, feq);
+#pragma unroll
+  for (int l = 0; l < L::Q; ++l) {
+    if ((miss >> l) & 1u) f[l] = f[opp<L>(l)] + feq[l] - feq[opp<L>(l)];
+  }
+  if (kind == BC_REG_V || kind == BC_REG_P) {
+    T fneq[L::Q];
+#pragma unroll
+    for (int l = 0; l < L::Q; ++l) fneq[l] = f[l] - feq[l];
+    T pi[L::NT];
+    second_moment<L>(fneq, pi);
+#pragma unroll
+    for (int l = 0; l < L::Q; ++l) {
+      T acc = T(0);
+#pragma unroll
+      for (int t = 0; t < L::NT; ++t) {
+        if (qi<L>(l, t) != 0.0) acc = acc + T(qi<L>(l, t)) * pi[t];
+      }
+      f[l] = feq[l] + T(4.5) * T(weight<L>(l)) * acc;
+    }
+  }
+}
+
+}  // namespace xlbg

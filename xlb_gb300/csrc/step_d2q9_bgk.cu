@@ -1,0 +1,8 @@
+// Fused step kernels for D2Q9 with BGK collision.
+#include "step_dispatch.cuh"
+
+namespace xlbg {
+int launch_step_d2q9_bgk(const StepArgs& a, int sk, int compute, bool fullbc, bool diag, cudaStream_t s) {
+  return launch_step_t<0, 0>(a, sk, compute, fullbc, diag, s);
+}
+}  // namespace xlbg

@@ -1,0 +1,8 @@
+// Fused step kernels for D3Q27 with KBC collision.
+#include "step_dispatch.cuh"
+
+namespace xlbg {
+int launch_step_d3q27_kbc(const StepArgs& a, int sk, int compute, bool fullbc, bool diag, cudaStream_t s) {
+  return launch_step_t<2, 1>(a, sk, compute, fullbc, diag, s);
+}
+}  // namespace xlbg

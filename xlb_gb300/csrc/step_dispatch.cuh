@@ -1,0 +1,50 @@
+// Launch of the fused step kernel for one (lattice, collision) pair.  Each
+// step_*.cu translation unit instantiates one pair so the build parallelises.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "step_kernel.cuh"
+
+namespace xlbg {
+
+// Returns 0 on launch, -1 for an unsupported store/compute pair, or the CUDA error.
+template <int LAT, int COLL>
+int launch_step_t(const StepArgs& a, int sk, int compute, bool fullbc, bool diag, cudaStream_t s) {
+  using L = Lattice<LAT>;
+  const dim3 grid((unsigned)(a.n0 * a.n1), (unsigned)((a.n2 + kStepBlock - 1) / kStepBlock));
+#define XLBG_LAUNCH(SKV, TV)                                                         \
+  do {                                                                               \
+    if (diag)                                                                        \
+      step_kernel<L, SKV, TV, COLL, true, true><<<grid, kStepBlock, 0, s>>>(a);     \
+    else if (fullbc)                                                                 \
+      step_kernel<L, SKV, TV, COLL, true, false><<<grid, kStepBlock, 0, s>>>(a);    \
+    else                                                                             \
+      step_kernel<L, SKV, TV, COLL, false, false><<<grid, kStepBlock, 0, s>>>(a);   \
+  } while (0)
+  if (compute == 1) {
+    switch (sk) {
+      case SK_F64: XLBG_LAUNCH(SK_F64, double); break;
+      case SK_F32: XLBG_LAUNCH(SK_F32, double); break;
+      case SK_F16: XLBG_LAUNCH(SK_F16, double); break;
+      default: return -1;
+    }
+  } else {
+    switch (sk) {
+      case SK_F32: XLBG_LAUNCH(SK_F32, float); break;
+      case SK_F16: XLBG_LAUNCH(SK_F16, float); break;
+      case SK_F16S: XLBG_LAUNCH(SK_F16S, float); break;
+      case SK_BF16S: XLBG_LAUNCH(SK_BF16S, float); break;
+      default: return -1;
+    }
+  }
+#undef XLBG_LAUNCH
+  return (int)cudaGetLastError();
+}
+
+int launch_step_d2q9_bgk(const StepArgs&, int, int, bool, bool, cudaStream_t);
+int launch_step_d2q9_kbc(const StepArgs&, int, int, bool, bool, cudaStream_t);
+int launch_step_d3q19_bgk(const StepArgs&, int, int, bool, bool, cudaStream_t);
+int launch_step_d3q27_bgk(const StepArgs&, int, int, bool, bool, cudaStream_t);
+int launch_step_d3q27_kbc(const StepArgs&, int, int, bool, bool, cudaStream_t);
+
+}  // namespace xlbg

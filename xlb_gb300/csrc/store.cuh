@@ -1,0 +1,82 @@
+// Store forms of the population fields.
+//
+// XLB casts to the compute type on load and to the store type on store
+// (nse_stepper.py:309-310, :381, stream.py:80).  The shifted forms keep
+// f - w_l in FP16 / BF16 and add w_l back on load; all conversions are the
+// CUDA round-to-nearest-even intrinsics.  "raw" loads/stores are for boundary
+// aux values, which are not populations and are never shifted.
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+namespace xlbg {
+
+enum { SK_F32 = 0, SK_F64 = 1, SK_F16 = 2, SK_F16S = 3, SK_BF16S = 4 };
+
+template <int SK, class T>
+struct Store;
+
+template <class T>
+struct Store<SK_F32, T> {
+  using S = float;
+  using Bits = uint32_t;
+  static constexpr bool shifted = false;
+  __device__ static __forceinline__ T dec(Bits b, T) { return (T)__uint_as_float(b); }
+  __device__ static __forceinline__ Bits enc(T v, T) { return __float_as_uint((float)v); }
+  __device__ static __forceinline__ T dec_raw(Bits b) { return (T)__uint_as_float(b); }
+};
+
+template <class T>
+struct Store<SK_F64, T> {
+  using S = double;
+  using Bits = unsigned long long;
+  static constexpr bool shifted = false;
+  __device__ static __forceinline__ T dec(Bits b, T) { return (T)__longlong_as_double((long long)b); }
+  __device__ static __forceinline__ Bits enc(T v, T) { return (Bits)__double_as_longlong((double)v); }
+  __device__ static __forceinline__ T dec_raw(Bits b) { return (T)__longlong_as_double((long long)b); }
+};
+
+__device__ __forceinline__ __half to_half(float v) { return __float2half_rn(v); }
+__device__ __forceinline__ __half to_half(double v) { return __double2half(v); }
+
+template <class T>
+struct Store<SK_F16, T> {
+  using S = __half;
+  using Bits = unsigned short;
+  static constexpr bool shifted = false;
+  __device__ static __forceinline__ T dec(Bits b, T) { return (T)__half2float(__ushort_as_half(b)); }
+  __device__ static __forceinline__ Bits enc(T v, T) { return __half_as_ushort(to_half(v)); }
+  __device__ static __forceinline__ T dec_raw(Bits b) { return (T)__half2float(__ushort_as_half(b)); }
+};
+
+template <>
+struct Store<SK_F16S, float> {
+  using S = __half;
+  using Bits = unsigned short;
+  static constexpr bool shifted = true;
+  __device__ static __forceinline__ float dec(Bits b, float w) { return __half2float(__ushort_as_half(b)) + w; }
+  __device__ static __forceinline__ Bits enc(float v, float w) { return __half_as_ushort(__float2half_rn(v - w)); }
+  __device__ static __forceinline__ float dec_raw(Bits b) { return __half2float(__ushort_as_half(b)); }
+};
+
+template <>
+struct Store<SK_BF16S, float> {
+  using S = __nv_bfloat16;
+  using Bits = unsigned short;
+  static constexpr bool shifted = true;
+  __device__ static __forceinline__ float dec(Bits b, float w) {
+    return __bfloat162float(__ushort_as_bfloat16(b)) + w;
+  }
+  __device__ static __forceinline__ Bits enc(float v, float w) {
+    return __bfloat16_as_ushort(__float2bfloat16_rn(v - w));
+  }
+  __device__ static __forceinline__ float dec_raw(Bits b) { return __bfloat162float(__ushort_as_bfloat16(b)); }
+};
+
+template <class Bits>
+__device__ __forceinline__ Bits ldg_bits(const Bits* p) {
+  return __ldg(p);
+}
+
+}  // namespace xlbg

@@ -1,0 +1,3 @@
+from xlb_gb300.operator.stepper.nse_stepper import IncompressibleNavierStokesStepper, Stepper
+
+__all__ = ["IncompressibleNavierStokesStepper", "Stepper"]
