@@ -145,6 +145,28 @@ int xlbg_step_diag(const xlbg_desc* desc, void* f0, void* f1, const uint8_t* bc_
                    int32_t force_id, double* diag_slots, double* diag, void* stream);
 
 /*
+ * xlbg_step_diag without scratch arguments and without any device allocation.
+ * No counterpart in XLB: it exists for callers that cannot allocate device
+ * memory around a step -- hosts whose own pool owns the device heap and hand a
+ * library only the buffers it reads and writes, and loops that must not call
+ * cudaMalloc/cudaFree because those can synchronise the device.
+ *
+ * Its scratch (the reduction slots and the aux-recovery staging) lives in
+ * file-scope __device__ arrays of libxlbg.so, about 4 MiB held by every GPU
+ * that loads the library until the process exits.  n_rec * Q * store-bytes
+ * must not exceed XLBG_NOALLOC_REC_SCRATCH_BYTES (XLBG_ERR_ARG otherwise).
+ * The first call on a device looks up the arrays' device addresses
+ * (cudaGetSymbolAddress) for the calling thread's current device; make that
+ * first call before any stream capture.  The arrays are shared by all calls on
+ * a device: calls whose GPU work may overlap race on them and must be
+ * serialised by the caller.  Same results as xlbg_step_diag.
+ */
+#define XLBG_NOALLOC_REC_SCRATCH_BYTES (4u << 20)
+int xlbg_step_diag_noalloc(const xlbg_desc* desc, void* f0, void* f1, const uint8_t* bc_mask,
+                           const uint32_t* miss_bits, const int64_t* rec_cells, int64_t n_rec, double omega,
+                           int32_t timestep, int32_t force_id, double* diag, void* stream);
+
+/*
  * f = feq(rho, u) in the store form for every cell (initializers.py:5-20 with
  * quadratic_equilibrium.py:63-82).  rho: (1, cells) and u: (d, cells) in the
  * compute type, or NULL for the uniform values rho0 / u0[d].

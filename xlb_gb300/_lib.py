@@ -15,6 +15,7 @@ LIB_PATH = os.path.join(HERE, "lib", "libxlbg.so")
 ABI_VERSION = 1
 MAX_BC = 16
 DIAG_SLOTS = 1024
+NOALLOC_REC_SCRATCH_BYTES = 4 << 20
 
 OK, ERR_ARG, ERR_UNSUPPORTED, ERR_ALIGN, ERR_CUDA = 0, 1, 2, 3, 4
 
@@ -37,6 +38,7 @@ EXPORTED = (
     "xlbg_step",
     "xlbg_run",
     "xlbg_step_diag",
+    "xlbg_step_diag_noalloc",
     "xlbg_equilibrium",
     "xlbg_macroscopic",
 )
@@ -86,6 +88,7 @@ _SIGNATURES = {
     "xlbg_step": ([_DESC, _P, _P, _P, _P, _P, _I64, _P, _D, _I32, _P], ctypes.c_int),
     "xlbg_run": ([_DESC, _P, _P, _P, _P, _P, _I64, _P, _D, _I32, _I32, _P], ctypes.c_int),
     "xlbg_step_diag": ([_DESC, _P, _P, _P, _P, _P, _I64, _P, _D, _I32, _I32, _P, _P, _P], ctypes.c_int),
+    "xlbg_step_diag_noalloc": ([_DESC, _P, _P, _P, _P, _P, _I64, _D, _I32, _I32, _P, _P], ctypes.c_int),
     "xlbg_equilibrium": ([_DESC, _P, _P, _D, ctypes.POINTER(_D), _P, _P], ctypes.c_int),
     "xlbg_macroscopic": ([_DESC, _P, _P, _P, _P], ctypes.c_int),
 }

@@ -16,7 +16,7 @@ namespace xlbg {
 
 static thread_local std::string g_last_error;
 
-static int fail(int code, const char* fmt, ...) {
+int fail(int code, const char* fmt, ...) {
   char buf[512];
   va_list ap;
   va_start(ap, fmt);
@@ -31,7 +31,7 @@ static int cuda_status(cudaError_t e, const char* where) {
   return fail(XLBG_ERR_CUDA, "%s: %s", where, cudaGetErrorString(e));
 }
 
-static int store_bytes(int sk) { return sk == SK_F64 ? 8 : (sk == SK_F32 ? 4 : 2); }
+int store_bytes(int sk) { return sk == SK_F64 ? 8 : (sk == SK_F32 ? 4 : 2); }
 
 static int lattice_q(int lat) { return lat == 0 ? 9 : (lat == 1 ? 19 : 27); }
 static int lattice_d(int lat) { return lat == 0 ? 2 : 3; }
@@ -77,7 +77,7 @@ static int check_desc(const xlbg_desc* d) {
   return XLBG_OK;
 }
 
-static int check_ptr(const void* p, int align, const char* name) {
+int check_ptr(const void* p, int align, const char* name) {
   if (!p) return fail(XLBG_ERR_ARG, "%s is NULL", name);
   if (((uintptr_t)p) % (uintptr_t)align) return fail(XLBG_ERR_ALIGN, "%s is not %d-byte aligned", name, align);
   return XLBG_OK;
@@ -299,7 +299,7 @@ static int launch_main(const xlbg_desc* d, const StepArgs& a, bool diag, cudaStr
   return cuda_status((cudaError_t)r, "step kernel launch");
 }
 
-static int check_step_args(const xlbg_desc* d, const void* f0, const void* f1, const uint8_t* bc_mask,
+int check_step_args(const xlbg_desc* d, const void* f0, const void* f1, const uint8_t* bc_mask,
                            const uint32_t* miss, const int64_t* rec_cells, int64_t n_rec, const void* rec_scratch) {
   int e;
   if ((e = check_desc(d))) return e;
@@ -317,7 +317,7 @@ static int check_step_args(const xlbg_desc* d, const void* f0, const void* f1, c
   return XLBG_OK;
 }
 
-static int one_step(const xlbg_desc* d, void* f0, void* f1, const uint8_t* bc_mask, const uint32_t* miss,
+int one_step(const xlbg_desc* d, void* f0, void* f1, const uint8_t* bc_mask, const uint32_t* miss,
                     const int64_t* rec_cells, int64_t n_rec, void* rec_scratch, double omega, bool diag,
                     int force_id, double* slots, double* out, cudaStream_t s) {
   StepArgs a;
