@@ -27,7 +27,11 @@ Two places where XLB's Warp kernel is racy are given one deterministic meaning
 here, and the CUDA path implements the same meaning:
 
 1. Aux recovery (nse_stepper.py:338-342) writes f_0 while other threads pull
-   from f_0.  Here recovery happens after every pull of the step.
+   from f_0.  By default (``recovery="after"``) recovery happens after every
+   pull of the step; ``recovery="before"`` gives the other outcome, where other
+   cells' reads see the recovered slots (what a launch gives when the boundary
+   cells run first, and what XLB's source gives when run sequentially in cell
+   order for an inlet at x = 0).
 2. The masker (indices_boundary_masker.py:144-156) writes bc_mask from many
    threads; here boundary conditions are applied in list order, later wins.
 
@@ -448,17 +452,40 @@ def extrapolation_cs(T):
 # ----------------------------------------------------------------------------
 
 
-def step(lat, store, f0, f1, bc_mask, missing, omega, bcs, collision="BGK", T=np.float64):
+def _recovered(lat, f0, f1, bc_mask, missing, bcs, with_slot0=True):
+    """f0 with the aux-recovery writes of nse_stepper.py:318-342 applied."""
+    out = f0.copy()
+    for bc in bcs:
+        if bc.kind not in RECOVERY_KINDS:
+            continue
+        m = bc_mask[0] == bc.id
+        if with_slot0:
+            out[0][m] = f1[0][m]
+        for l in range(1, lat.q):
+            mm = m & missing[l]
+            o = lat.opp[l]
+            out[o][mm] = f1[o][mm]
+    return out
+
+
+def step(lat, store, f0, f1, bc_mask, missing, omega, bcs, collision="BGK", T=np.float64, recovery="after"):
     """One fused step.  Returns (f0_new, f1_new) as stored arrays.
 
     f0_new differs from f0 only where aux recovery wrote it
     (nse_stepper.py:318-342); f1_new holds the post-collision state except at
     cells with id 255, which the kernel skips (:356-358).
+
+    ``recovery`` resolves XLB's race between the recovery writes into f0 and
+    other cells' reads of f0: "after" (the CUDA path's order) lets every read
+    of the step see the pre-step f0; "before" lets reads of *other* cells see
+    the recovered slots, which is what a launch gives when the ZouHe /
+    Regularized cells run before the cells reading them.
     """
     shp = f0.shape[1:]
     ids = bc_mask[0]
     f0c = store.decode(f0, T)
-    fps = pull(lat, f0c)
+    f0r = f0c if recovery == "after" else store.decode(_recovered(lat, f0, f1, bc_mask, missing, bcs, with_slot0=False), T)
+    fps = pull(lat, f0r)
     omega_t = T(omega)
     by_id = {bc.id: bc for bc in bcs}
 
@@ -514,7 +541,7 @@ def step(lat, store, f0, f1, bc_mask, missing, omega, bcs, collision="BGK", T=np
                 src = cells[:, sel].copy()
                 for d in range(lat.d):
                     src[d] = (src[d] - (lat.c[d, l] + nv[d, sel])) % shp[d]
-                f_aux = f0c[l][tuple(src)]
+                f_aux = f0r[l][tuple(src)]
                 fo[lat.opp[l], sel] = (T(1.0) - cs) * fp[l, sel] + cs * f_aux
             fout[:, m] = fo
 
@@ -523,25 +550,15 @@ def step(lat, store, f0, f1, bc_mask, missing, omega, bcs, collision="BGK", T=np
     if skip.any():
         f1_new[:, skip] = f1[:, skip]
 
-    f0_new = f0.copy()
-    for bc in bcs:
-        if bc.kind not in RECOVERY_KINDS:
-            continue
-        m = ids == bc.id
-        f0_new[0][m] = f1[0][m]
-        for l in range(1, lat.q):
-            mm = m & missing[l]
-            o = lat.opp[l]
-            f0_new[o][mm] = f1[o][mm]
-    return f0_new, f1_new
+    return _recovered(lat, f0, f1, bc_mask, missing, bcs), f1_new
 
 
-def run(lat, store, f0, f1, bc_mask, missing, omega, bcs, steps, collision="BGK", T=np.float64):
+def run(lat, store, f0, f1, bc_mask, missing, omega, bcs, steps, collision="BGK", T=np.float64, recovery="after"):
     """``steps`` steps with the caller-side swap of XLB's examples
     (mlups_3d.py:78-80).  Returns (f_0, f_1) after the final swap: f_0 holds the
     newest state."""
     for _ in range(steps):
-        f0, f1 = step(lat, store, f0, f1, bc_mask, missing, omega, bcs, collision, T)
+        f0, f1 = step(lat, store, f0, f1, bc_mask, missing, omega, bcs, collision, T, recovery)
         f0, f1 = f1, f0
     return f0, f1
 

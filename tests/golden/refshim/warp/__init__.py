@@ -1,0 +1,336 @@
+"""A minimal CPU emulation of the NVIDIA Warp Python API, enough to execute XLB's
+Warp stepper source unmodified for golden-vector generation.
+
+Test infrastructure only (used by tests/golden/make_golden.py in the container
+that holds the XLB source tree).  Semantics modelled:
+
+* ``wp.vec`` / ``wp.mat`` value types with element dtype (numpy scalars, so FP64
+  arithmetic is IEEE double, op by op, no fusion);
+* ``@wp.func`` passes vectors by value (arguments are copied on entry);
+* ``@wp.kernel`` + ``wp.launch`` run the kernel body once per thread index, in
+  row-major order, sequentially;
+* ``wp.static``, ``wp.constant`` are identities;
+* builtins used by XLB's stepper path: dot, cw_div, abs, sqrt, atomic_add, tid.
+
+Python-scope builtin calls on Python floats (``wp.sqrt(3.0)``) evaluate in
+float32, the way Warp types bare Python floats.  Kernel scalar arguments keep
+their Python type (Warp would type a bare float as float32; this emulator does
+not model that).
+"""
+
+import itertools
+
+import numpy as np
+
+float16 = np.float16
+float32 = np.float32
+float64 = np.float64
+int8 = np.int8
+int32 = np.int32
+int64 = np.int64
+uint8 = np.uint8
+uint32 = np.uint32
+bool = np.bool_  # noqa: A001  (Warp's name)
+
+_vec_types = {}
+
+
+class _Vec:
+    __array_ufunc__ = None  # make numpy scalars defer to our reflected operators
+    length = 0
+    dtype = float32
+
+    def __init__(self, *args):
+        n, dt = self.length, self.dtype
+        if not args:
+            vals = [dt(0)] * n
+        elif len(args) == 1 and hasattr(args[0], "__len__") and not isinstance(args[0], str):
+            vals = [dt(v) for v in args[0]]
+        else:
+            vals = [dt(v) for v in args]
+        if len(vals) != n:
+            raise ValueError(f"vector of length {n} built from {len(vals)} values")
+        self.v = vals
+
+    def copy(self):
+        c = type(self).__new__(type(self))
+        c.v = list(self.v)
+        return c
+
+    def __len__(self):
+        return self.length
+
+    def __iter__(self):
+        return iter(self.v)
+
+    def __getitem__(self, i):
+        return self.v[int(i)]
+
+    def __setitem__(self, i, x):
+        self.v[int(i)] = self.dtype(x)
+
+    def _map(self, fn):
+        c = type(self).__new__(type(self))
+        c.v = [self.dtype(fn(a)) for a in self.v]
+        return c
+
+    def _zip(self, other, fn):
+        c = type(self).__new__(type(self))
+        c.v = [self.dtype(fn(a, b)) for a, b in zip(self.v, other.v)]
+        return c
+
+    def __add__(self, o):
+        return self._zip(o, lambda a, b: a + b) if isinstance(o, _Vec) else self._map(lambda a: a + o)
+
+    def __sub__(self, o):
+        return self._zip(o, lambda a, b: a - b) if isinstance(o, _Vec) else self._map(lambda a: a - o)
+
+    def __mul__(self, o):
+        if isinstance(o, _Vec):
+            raise TypeError("vec * vec is not defined; use wp.cw_mul")
+        return self._map(lambda a: a * o)
+
+    def __rmul__(self, o):
+        return self._map(lambda a: o * a)
+
+    def __truediv__(self, o):
+        return self._map(lambda a: a / o)
+
+    def __neg__(self):
+        return self._map(lambda a: -a)
+
+    def __repr__(self):
+        return f"vec{self.length}({', '.join(map(str, self.v))})"
+
+
+def _vec_type(length, dtype):
+    key = (int(length), dtype)
+    if key not in _vec_types:
+        _vec_types[key] = type(f"vec{length}_{getattr(dtype, '__name__', dtype)}", (_Vec,), {"length": int(length), "dtype": dtype})
+    return _vec_types[key]
+
+
+def vec(*args, length=None, dtype=None):
+    """``wp.vec(length, dtype)`` is a type; ``wp.vec(value, length=n)`` a value."""
+    if length is None:
+        return _vec_type(args[0], dtype)
+    if not args:
+        return _vec_type(length, dtype)
+    dt = dtype or (type(args[0]) if isinstance(args[0], np.generic) else float32)
+    return _vec_type(length, dt)(*args)
+
+
+vec2i = _vec_type(2, int32)
+vec3i = _vec_type(3, int32)
+vec2f = _vec_type(2, float32)
+vec3f = _vec_type(3, float32)
+vec2d = _vec_type(2, float64)
+vec3d = _vec_type(3, float64)
+vec3 = vec3f
+vec2 = vec2f
+
+
+class _Mat:
+    __array_ufunc__ = None
+
+    def __init__(self, a, dtype):
+        self.a = np.asarray(a).astype(dtype)
+        self.dtype = dtype
+
+    def __getitem__(self, idx):
+        if isinstance(idx, tuple):
+            return self.a[tuple(int(i) for i in idx)]
+        return _vec_type(self.a.shape[1], self.dtype)(self.a[int(idx)])
+
+
+def mat(shape, dtype=float32):
+    def make(a):
+        m = _Mat(a, dtype)
+        if m.a.shape != tuple(shape):
+            raise ValueError(f"matrix data of shape {m.a.shape}, type is {tuple(shape)}")
+        return m
+
+    return make
+
+
+# ----------------------------------------------------------------------------- arrays
+
+
+class _Array(np.ndarray):
+    """numpy array with Warp's ``.numpy()``."""
+
+    def numpy(self):
+        return np.asarray(self)
+
+
+class _VecArray:
+    """1-D array whose elements are vectors (``wp.zeros(n, dtype=vec_type)``)."""
+
+    def __init__(self, n, vt):
+        self.data = [vt() for _ in range(n)]
+        self.shape = (n,)
+
+    def __getitem__(self, i):
+        return self.data[int(i)]
+
+    def __setitem__(self, i, x):
+        self.data[int(i)] = x
+
+    def numpy(self):
+        return np.array([v.v for v in self.data])
+
+
+def _as_array(a, dtype=None):
+    arr = np.asarray(a) if dtype is None else np.asarray(a).astype(dtype)
+    return np.ascontiguousarray(arr).view(_Array)
+
+
+def array(data=None, dtype=None, shape=None, device=None, **kw):
+    """``wp.array(data, dtype)`` copies ``data``; ``wp.array(dtype=...)`` alone is an annotation."""
+    if data is None:
+        return None
+    return _as_array(data, dtype)
+
+
+def _annotation(*a, **k):
+    return None
+
+
+array1d = array2d = array3d = array4d = _annotation
+
+
+def zeros(shape, dtype=float32, device=None, **kw):
+    if isinstance(dtype, type) and issubclass(dtype, _Vec):
+        n = shape if isinstance(shape, int) else int(np.prod(shape))
+        return _VecArray(n, dtype)
+    return np.zeros(shape, dtype=dtype).view(_Array)
+
+
+def full(shape, value, dtype=float32, device=None, **kw):
+    return np.full(shape, value, dtype=dtype).view(_Array)
+
+
+def copy(dest, src, *a, **k):
+    dest[...] = src
+
+
+def from_numpy(a, dtype=None, **kw):
+    return _as_array(a, dtype)
+
+
+# ----------------------------------------------------------------------------- functions and kernels
+
+
+def func(f):
+    def call(*args, **kwargs):
+        args = [a.copy() if isinstance(a, _Vec) else a for a in args]
+        return f(*args, **kwargs)
+
+    call.__wrapped__ = f
+    call.__name__ = getattr(f, "__name__", "func")
+    return call
+
+
+def kernel(f=None, **kw):
+    if f is None:
+        return lambda g: g
+    return f
+
+
+_current_tid = None
+
+
+def tid():
+    return _current_tid
+
+
+def launch(kernel, dim, inputs=(), outputs=(), device=None, **kw):
+    global _current_tid
+    args = list(inputs) + list(outputs)
+    if isinstance(dim, (int, np.integer)):
+        it = ((i,) for i in range(int(dim)))
+        single = True
+    else:
+        it = itertools.product(*[range(int(d)) for d in dim])
+        single = False
+    try:
+        for t in it:
+            _current_tid = t[0] if single else tuple(int32(v) for v in t)
+            kernel(*args)
+    finally:
+        _current_tid = None
+
+
+def static(x):
+    return x
+
+
+def constant(x):
+    return x
+
+
+def init():
+    return None
+
+
+def synchronize():
+    return None
+
+
+# ----------------------------------------------------------------------------- builtins
+
+
+def dot(a, b):
+    s = a.dtype(0)
+    for x, y in zip(a.v, b.v):
+        s = s + x * y
+    return s
+
+
+def cw_div(a, b):
+    return a._zip(b, lambda x, y: x / y)
+
+
+def cw_mul(a, b):
+    return a._zip(b, lambda x, y: x * y)
+
+
+def abs(x):  # noqa: A001
+    return np.abs(x)
+
+
+def sqrt(x):
+    if isinstance(x, float):  # Python-scope call on a bare float: float32 in Warp
+        return float(np.sqrt(np.float32(x)))
+    return np.sqrt(x)
+
+
+def max(a, b):  # noqa: A001
+    return a if a >= b else b
+
+
+def min(a, b):  # noqa: A001
+    return a if a <= b else b
+
+
+def length(v):
+    return np.sqrt(dot(v, v))
+
+
+def atomic_add(arr, i, value):
+    arr[i] = arr[i] + value
+    return arr[i]
+
+
+class _Permissive:
+    """Stand-in for Warp names the stepper path never calls (import-time only)."""
+
+    def __call__(self, *a, **k):
+        return self
+
+    def __getattr__(self, name):
+        return self
+
+
+def __getattr__(name):
+    return _Permissive()
