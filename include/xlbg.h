@@ -3,7 +3,7 @@
  *
  * Every entry point takes plain device pointers, sizes and a CUDA stream
  * (cudaStream_t passed as void*), returns an int status (XLBG_OK == 0) and
- * never allocates device memory.  Launches are asynchronous on the given
+ * never calls cudaMalloc or cudaFree.  Launches are asynchronous on the given
  * stream; nothing synchronises.  The last error message of the calling thread
  * is available from xlbg_last_error().
  *
@@ -50,8 +50,11 @@ enum {
 };
 enum { XLBG_COMPUTE_F32 = 0, XLBG_COMPUTE_F64 = 1 };
 
-/* collision (xlb/operator/collision/bgk.py:30-34, kbc.py:192-296) */
-enum { XLBG_BGK = 0, XLBG_KBC = 1 };
+/* collision (xlb/operator/collision/bgk.py:30-34, kbc.py:192-296).  XLBG_BGK_PAIR is BGK
+   with macroscopic and equilibrium rearranged over opposite-direction pairs (one
+   reciprocal for u, shared pair terms): the same equations with fewer operations,
+   results equal to XLBG_BGK up to rounding.  No XLB counterpart. */
+enum { XLBG_BGK = 0, XLBG_KBC = 1, XLBG_BGK_PAIR = 2 };
 
 /* boundary-condition kinds (xlb/operator/boundary_condition/bc_*.py) */
 enum {
@@ -82,7 +85,7 @@ typedef struct {
   int32_t lattice;     /* XLBG_D2Q9 / XLBG_D3Q19 / XLBG_D3Q27 */
   int32_t store;       /* XLBG_STORE_* */
   int32_t compute;     /* XLBG_COMPUTE_* */
-  int32_t collision;   /* XLBG_BGK / XLBG_KBC */
+  int32_t collision;   /* XLBG_BGK / XLBG_KBC / XLBG_BGK_PAIR */
   int32_t nbc;         /* entries used in bc[] */
   int64_t nx, ny, nz;  /* grid shape; nz = 1 for 2D */
   xlbg_bc bc[XLBG_MAX_BC];

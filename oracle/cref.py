@@ -45,7 +45,7 @@ class Stepper:
     def __init__(self, lat, shape, bc_mask, missing, bcs, collision="BGK", T=np.float32, threads=0):
         self.lat, self.T, self.threads = lat, T, threads
         self.s3 = tuple(shape) if len(shape) == 3 else tuple(shape) + (1,)
-        self.collision = 0 if collision == "BGK" else 1
+        self.collision = {"BGK": 0, "KBC": 1, "BGK_PAIR": 2}[collision]
         self.bc_mask = np.ascontiguousarray(bc_mask, dtype=np.uint8)
         bits = np.zeros(self.s3, dtype=np.uint32)
         for l in range(lat.q):

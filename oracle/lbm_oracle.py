@@ -314,6 +314,50 @@ def bgk(f, feq, omega_t):
     return f - omega_t * (f - feq)
 
 
+def bgk_pair(lat, f, omega_t, T):
+    """BGK with macroscopic and equilibrium arranged over opposite-direction pairs
+    (collision code 2; no XLB counterpart).  Same equations as macroscopic +
+    equilibrium + bgk; the operation order below is the CUDA path's."""
+    pairs = [l for l in range(1, lat.q) if l < lat.opp[l]]
+    rho = f[0].copy()
+    j = [np.zeros_like(rho) for _ in range(lat.d)]
+    for l in pairs:
+        o = lat.opp[l]
+        sig = f[l] + f[o]
+        dif = f[l] - f[o]
+        rho = rho + sig
+        for d in range(lat.d):
+            if lat.c[d, l] == 1:
+                j[d] = j[d] + dif
+            elif lat.c[d, l] == -1:
+                j[d] = j[d] - dif
+    inv = T(1.0) / rho
+    u = [jd * inv for jd in j]
+    usq = u[0] * u[0]
+    for d in range(1, lat.d):
+        usq = usq + u[d] * u[d]
+    base = T(1.0) - T(1.5) * usq
+    omf = T(1.0) - omega_t
+    orho = omega_t * rho
+    w = lat.w.astype(T)
+    fo = np.empty_like(f)
+    fo[0] = omf * f[0] + orho * w[0] * base
+    for l in pairs:
+        o = lat.opp[l]
+        cu = np.zeros_like(rho)
+        for d in range(lat.d):
+            if lat.c[d, l] == 1:
+                cu = cu + u[d]
+            elif lat.c[d, l] == -1:
+                cu = cu - u[d]
+        e = base + T(4.5) * (cu * cu)
+        t = T(3.0) * cu
+        ow = orho * w[l]
+        fo[l] = omf * f[l] + ow * (e + t)
+        fo[o] = omf * f[o] + ow * (e - t)
+    return fo
+
+
 def second_moment(lat, fneq, T):
     nt = lat.d * (lat.d + 1) // 2
     pi = []
@@ -511,14 +555,17 @@ def step(lat, store, f0, f1, bc_mask, missing, omega, bcs, collision="BGK", T=np
             fp = zouhe_like(lat, fp, miss, aux, bc.kind, T)
         fps[:, m] = fp
 
-    rho, u = macroscopic(lat, fps, T)
-    feq = equilibrium(lat, rho, u, T)
-    if collision == "BGK":
-        fout = bgk(fps, feq, omega_t)
-    elif collision == "KBC":
-        fout = kbc(lat, fps, feq, rho, omega_t, T)
+    if collision == "BGK_PAIR":
+        fout = bgk_pair(lat, fps, omega_t, T)
     else:
-        raise ValueError(collision)
+        rho, u = macroscopic(lat, fps, T)
+        feq = equilibrium(lat, rho, u, T)
+        if collision == "BGK":
+            fout = bgk(fps, feq, omega_t)
+        elif collision == "KBC":
+            fout = kbc(lat, fps, feq, rho, omega_t, T)
+        else:
+            raise ValueError(collision)
 
     # collision-step BCs and the extrapolation aux data (nse_stepper.py:286-293)
     for bc in bcs:

@@ -83,6 +83,38 @@ static void FN(kbc)(const lattice_t* L, const T* f, const T* feq, T rho, T omega
   for (int l = 0; l < L->q; ++l) fo[l] = f[l] - beta * (two * ds[l] + gamma * dh[l]);
 }
 
+static void FN(bgk_pair)(const lattice_t* L, const T* f, T omega, T* fo) {
+  T rho = f[0], j[3] = {(T)0, (T)0, (T)0}, u[3];
+  for (int l = 1; l < L->q; ++l) {
+    const int o = L->opp[l];
+    if (l >= o) continue;
+    const T sig = f[l] + f[o], dif = f[l] - f[o];
+    rho = rho + sig;
+    for (int d = 0; d < L->d; ++d) {
+      if (L->c[l][d] == 1) j[d] = j[d] + dif;
+      if (L->c[l][d] == -1) j[d] = j[d] - dif;
+    }
+  }
+  const T inv = (T)1 / rho;
+  for (int d = 0; d < L->d; ++d) u[d] = j[d] * inv;
+  T usq = u[0] * u[0];
+  for (int d = 1; d < L->d; ++d) usq = usq + u[d] * u[d];
+  const T base = (T)1 - (T)1.5 * usq, omf = (T)1 - omega, orho = omega * rho;
+  fo[0] = omf * f[0] + orho * (T)L->w[0] * base;
+  for (int l = 1; l < L->q; ++l) {
+    const int o = L->opp[l];
+    if (l >= o) continue;
+    T cu = (T)0;
+    for (int d = 0; d < L->d; ++d) {
+      if (L->c[l][d] == 1) cu = cu + u[d];
+      if (L->c[l][d] == -1) cu = cu - u[d];
+    }
+    const T e = base + (T)4.5 * (cu * cu), t = (T)3 * cu, ow = orho * (T)L->w[l];
+    fo[l] = omf * f[l] + ow * (e + t);
+    fo[o] = omf * f[o] + ow * (e - t);
+  }
+}
+
 static void FN(normal)(const lattice_t* L, uint32_t miss, int* nv) {
   for (int d = 0; d < L->d; ++d) nv[d] = 0;
   for (int l = 0; l < L->q; ++l) {
@@ -204,12 +236,16 @@ int FN(lbm_ref_step)(int lattice, int collision, int64_t nx, int64_t ny, int64_t
       } else if (kind >= BC_ZOUHE_V && kind <= BC_REG_P) {
         FN(zouhe_like)(L, f, m, f1[cell], kind);
       }
-      FN(macroscopic)(L, f, &rho, u);
-      FN(equilibrium)(L, rho, u, feq);
-      if (collision == 0) {
-        for (int l = 0; l < Q; ++l) fo[l] = f[l] - omega * (f[l] - feq[l]);
+      if (collision == 2) {
+        FN(bgk_pair)(L, f, omega, fo);
       } else {
-        FN(kbc)(L, f, feq, rho, omega, fo);
+        FN(macroscopic)(L, f, &rho, u);
+        FN(equilibrium)(L, rho, u, feq);
+        if (collision == 0) {
+          for (int l = 0; l < Q; ++l) fo[l] = f[l] - omega * (f[l] - feq[l]);
+        } else {
+          FN(kbc)(L, f, feq, rho, omega, fo);
+        }
       }
       if (kind == BC_FULLWAY) {
         for (int l = 0; l < Q; ++l) fo[l] = f[L->opp[l]];

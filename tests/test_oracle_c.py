@@ -41,3 +41,13 @@ def test_c_oracle_skip_cells():
     got0, got1 = st.run(sc.f0.copy(), sc.f1.copy(), sc.omega, 2)
     assert np.array_equal(got0, want0) and np.array_equal(got1, want1)
     assert O is not None
+
+
+@pytest.mark.parametrize("lattice,shape,layout", [("D3Q19", (16, 10, 10), "channel_regularized"), ("D2Q9", (30, 18), "channel_zouhe")])
+def test_c_oracle_pair_form(lattice, shape, layout):
+    sc = Scenario(lattice, shape, layout, policy="fp32", collision="BGK_PAIR")
+    sc.randomize(seed=12)
+    want0, want1 = sc.oracle_steps(3)
+    st = cref.Stepper(sc.lat, shape, sc.bc_mask, sc.missing, sc.obcs, "BGK_PAIR", sc.T, threads=2)
+    got0, got1 = st.run(sc.f0.copy(), sc.f1.copy(), sc.omega, 3)
+    assert np.array_equal(got0, want0) and np.array_equal(got1, want1)

@@ -246,3 +246,16 @@ def test_fp32_oracle_tracks_fp64(lat):
     f32 = f64.astype(np.float32)
     a32, _ = O.run(L, O.Store("f32", L), f32, f32.copy(), bcm, miss, 1.6, bcs, 10, T=np.float32)
     assert np.max(np.abs(a32 - a64)) < 2e-6
+
+
+@pytest.mark.parametrize("lat", LATS)
+def test_bgk_pair_form_equals_bgk_to_rounding(lat):
+    """The pair form rearranges macroscopic + equilibrium + BGK; in FP64 it agrees
+    with XLB's operation order to rounding."""
+    L = O.Lattice(lat)
+    rng = np.random.default_rng(11)
+    f = L.w[:, None] * (1 + 0.2 * rng.uniform(-1, 1, (L.q, 200)))
+    rho, u = O.macroscopic(L, f, np.float64)
+    want = O.bgk(f, O.equilibrium(L, rho, u, np.float64), 1.7)
+    got = O.bgk_pair(L, f, 1.7, np.float64)
+    assert np.max(np.abs(got - want)) < 1e-15

@@ -114,3 +114,57 @@ def test_prepare_fields_matches_oracle(lattice, shape, layout):
     _compare(missing.cpu().numpy(), sc.missing, "missing_mask")
     _compare(sc.to_numpy(f_0), sc.f0, "f_0 init")
     _compare(sc.to_numpy(f_1), sc.f1, "f_1 init with aux")
+
+
+# Shapes whose contiguous extent (nz, or ny in 2D) is divisible by 2 and 4, so the
+# V-cells-per-thread kernel runs (V = 2 for 4/8-byte stores, V = 4 for 2-byte
+# stores), with several warps per row and a partial last warp.
+VEC_CASES = [
+    ("D3Q19", (6, 5, 136), "cavity_fullway"),
+    ("D3Q19", (8, 6, 68), "channel_regularized"),
+    ("D3Q19", (7, 6, 264), "channel_zouhe"),
+    ("D2Q9", (10, 260), "channel_zouhe"),
+    ("D2Q9", (9, 1028), "cavity_halfway"),
+    ("D3Q27", (6, 5, 40), "cavity_halfway"),
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("policy", ["fp32", "fp64", "f16s", "bf16s", "f16"])
+@pytest.mark.parametrize("lattice,shape,layout", VEC_CASES)
+def test_vector_kernel_matches_oracle(lattice, shape, layout, policy):
+    sc = Scenario(lattice, shape, layout, policy=policy, collision="BGK")
+    sc.randomize(seed=7)
+    want0, want1 = sc.oracle_steps(3)
+    got0, got1 = sc.gpu_steps(3)
+    _compare(got0, want0, "f_0")
+    _compare(got1, want1, "f_1")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("policy", ["fp32", "f16s"])
+def test_vector_kernel_skip_cells(policy):
+    sc = Scenario("D3Q19", (6, 5, 136), "cavity_fullway", policy=policy)
+    sc.randomize(seed=8)
+    sc.bc_mask[0, 2:4, 1:3, 37:71] = 255
+    want0, want1 = sc.oracle_steps(2)
+    got0, got1 = sc.gpu_steps(2)
+    _compare(got0, want0, "f_0")
+    _compare(got1, want1, "f_1")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("policy", ["fp32", "fp64", "f16"])
+@pytest.mark.parametrize(
+    "lattice,shape,layout",
+    [("D2Q9", (30, 18), "channel_zouhe"), ("D3Q19", (16, 10, 10), "channel_regularized"),
+     ("D3Q19", (6, 5, 136), "cavity_fullway"), ("D3Q27", (12, 10, 9), "cavity_halfway")],
+)
+def test_bgk_pair_form_matches_oracle(lattice, shape, layout, policy):
+    """collision_type="BGK_PAIR" under the XLB policies (the shifted policies use it by default)."""
+    sc = Scenario(lattice, shape, layout, policy=policy, collision="BGK_PAIR")
+    sc.randomize(seed=9)
+    want0, want1 = sc.oracle_steps(3)
+    got0, got1 = sc.gpu_steps(3)
+    _compare(got0, want0, "f_0")
+    _compare(got1, want1, "f_1")

@@ -28,7 +28,7 @@ BC_REGULARIZED_VELOCITY = 6
 BC_REGULARIZED_PRESSURE = 7
 BC_EXTRAPOLATION = 8
 
-BGK, KBC = 0, 1
+BGK, KBC, BGK_PAIR = 0, 1, 2
 
 EXPORTED = (
     "xlbg_abi_version",

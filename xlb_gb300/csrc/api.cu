@@ -5,6 +5,7 @@
 #include <stdarg.h>
 #include <stdint.h>
 #include <stdio.h>
+#include <stdlib.h>
 
 #include <cmath>
 #include <string>
@@ -56,7 +57,7 @@ static int check_desc(const xlbg_desc* d) {
     return fail(XLBG_ERR_ARG, "unknown compute type %d", d->compute);
   if (d->compute == XLBG_COMPUTE_F64 && (d->store == XLBG_STORE_F16S || d->store == XLBG_STORE_BF16S))
     return fail(XLBG_ERR_UNSUPPORTED, "shifted FP16/BF16 storage is defined with FP32 compute only");
-  if (d->collision != XLBG_BGK && d->collision != XLBG_KBC)
+  if (d->collision != XLBG_BGK && d->collision != XLBG_KBC && d->collision != XLBG_BGK_PAIR)
     return fail(XLBG_ERR_ARG, "unknown collision %d", d->collision);
   if (d->collision == XLBG_KBC && d->lattice == XLBG_D3Q19)
     return fail(XLBG_ERR_UNSUPPORTED, "KBC collision is defined for D2Q9 and D3Q27 only (kbc.py:184-185)");
@@ -261,6 +262,7 @@ static int fill_step_args(const xlbg_desc* d, const void* f0, void* f1, const ui
   internal_dims(d, a.n0, a.n1, a.n2);
   a.nbc = d->nbc;
   a.omega = omega;
+  a.omega_f = (float)omega;
   // cs = compute_dtype(1.0 / wp.sqrt(3.0)) with wp.sqrt evaluated in float32 at
   // Python scope (bc_extrapolation_outflow.py:353)
   a.extrap_cs = 1.0 / (double)sqrtf(3.0f);
@@ -284,17 +286,50 @@ static int fill_step_args(const xlbg_desc* d, const void* f0, void* f1, const ui
   return XLBG_OK;
 }
 
+// Rows per thread of the marching kernel.  XLBG_CHUNK overrides it (0 selects
+// the one-cell-per-thread kernel); the default keeps at least eight blocks per
+// SM of a 152-SM GB300 and at most 64 rows per thread.
+static int choose_chunk(const StepArgs& a, int threads) {
+  static const int forced = [] {
+    const char* e = getenv("XLBG_CHUNK");
+    return e ? atoi(e) : -1;
+  }();
+  if (forced >= 0) return forced;
+  const long long columns = (long long)a.n0 * ((a.n2 + threads - 1) / threads);
+  long long chunk = (long long)a.n1 * columns / (152LL * 8);
+  if (chunk < 1) chunk = 1;
+  if (chunk > 64) chunk = 64;
+  return (int)chunk;
+}
+
 static int launch_main(const xlbg_desc* d, const StepArgs& a, bool diag, cudaStream_t s) {
   const bool full = needs_full_bc(d) || diag;
+  const bool pair = d->collision == XLBG_BGK_PAIR;
   int r = -1;
+  if (!diag && a.ncell < 0x7fffffffLL) {
+    const int threads = a.n2 >= kStepBlock ? kStepBlock : ((a.n2 + 31) / 32) * 32;
+    const int chunk = choose_chunk(a, threads);
+    if (chunk > 0) {
+      if (d->lattice == 0)
+        r = d->collision == XLBG_KBC ? launch_step_march_d2q9_kbc(a, d->store, d->compute, full, threads, chunk, s)
+                                     : launch_step_march_d2q9_bgk(a, d->store, d->compute, full, pair, threads, chunk, s);
+      else if (d->lattice == 1)
+        r = launch_step_march_d3q19_bgk(a, d->store, d->compute, full, pair, threads, chunk, s);
+      else
+        r = d->collision == XLBG_KBC ? launch_step_march_d3q27_kbc(a, d->store, d->compute, full, threads, chunk, s)
+                                     : launch_step_march_d3q27_bgk(a, d->store, d->compute, full, pair, threads, chunk, s);
+      if (r < 0) return fail(XLBG_ERR_UNSUPPORTED, "store/compute pair not supported");
+      return cuda_status((cudaError_t)r, "step kernel launch");
+    }
+  }
   if (d->lattice == 0)
-    r = d->collision == XLBG_BGK ? launch_step_d2q9_bgk(a, d->store, d->compute, full, diag, s)
-                                 : launch_step_d2q9_kbc(a, d->store, d->compute, full, diag, s);
+    r = d->collision == XLBG_KBC ? launch_step_d2q9_kbc(a, d->store, d->compute, full, diag, s)
+                                 : launch_step_d2q9_bgk(a, d->store, d->compute, full, diag, pair, s);
   else if (d->lattice == 1)
-    r = launch_step_d3q19_bgk(a, d->store, d->compute, full, diag, s);
+    r = launch_step_d3q19_bgk(a, d->store, d->compute, full, diag, pair, s);
   else
-    r = d->collision == XLBG_BGK ? launch_step_d3q27_bgk(a, d->store, d->compute, full, diag, s)
-                                 : launch_step_d3q27_kbc(a, d->store, d->compute, full, diag, s);
+    r = d->collision == XLBG_KBC ? launch_step_d3q27_kbc(a, d->store, d->compute, full, diag, s)
+                                 : launch_step_d3q27_bgk(a, d->store, d->compute, full, diag, pair, s);
   if (r < 0) return fail(XLBG_ERR_UNSUPPORTED, "store/compute pair not supported");
   return cuda_status((cudaError_t)r, "step kernel launch");
 }

@@ -33,22 +33,39 @@ __host__ __device__ constexpr int d2q9_c(int l, int k) {
 template <int LAT>
 struct Lattice;
 
+// Opposite directions in closed form, so constant arguments fold to immediates.
+// D3Q27: negate each base-3 digit (0 -> 0, 1 -> 2, 2 -> 1).
+__host__ __device__ constexpr int d3q27_opp(int l) {
+  return 9 * ((3 - l / 9) % 3) + 3 * ((3 - (l / 3) % 3) % 3) + (3 - l % 3) % 3;
+}
+
 template <>
 struct Lattice<0> {  // D2Q9
   static constexpr int Q = 9, D = 2, NT = 3;
   __host__ __device__ static constexpr int c(int l, int k) { return d2q9_c(l, k); }
+  // [0, 2, 1, 6, 5, 4, 3, 8, 7]
+  __host__ __device__ static constexpr int opp(int l) {
+    return l == 0 ? 0 : l == 1 ? 2 : l == 2 ? 1 : l == 3 ? 6 : l == 4 ? 5 : l == 5 ? 4 : l == 6 ? 3 : l == 7 ? 8 : 7;
+  }
 };
 
 template <>
 struct Lattice<1> {  // D3Q19
   static constexpr int Q = 19, D = 3, NT = 6;
   __host__ __device__ static constexpr int c(int l, int k) { return d3q27_c(d3q19_map(l), k); }
+  // [0, 2, 1, 6, 8, 7, 3, 5, 4, 14, 16, 15, 18, 17, 9, 11, 10, 13, 12]
+  __host__ __device__ static constexpr int opp(int l) {
+    return l < 9 ? d3q27_opp(l)
+                 : (l == 9 ? 14 : l == 10 ? 16 : l == 11 ? 15 : l == 12 ? 18 : l == 13 ? 17
+                    : l == 14 ? 9 : l == 15 ? 11 : l == 16 ? 10 : l == 17 ? 13 : 12);
+  }
 };
 
 template <>
 struct Lattice<2> {  // D3Q27
   static constexpr int Q = 27, D = 3, NT = 6;
   __host__ __device__ static constexpr int c(int l, int k) { return d3q27_c(l, k); }
+  __host__ __device__ static constexpr int opp(int l) { return d3q27_opp(l); }
 };
 
 template <class L>
@@ -69,13 +86,20 @@ __host__ __device__ constexpr double weight(int l) {
 
 template <class L>
 __host__ __device__ constexpr int opp(int l) {
-  for (int m = 0; m < L::Q; ++m) {
-    bool same = true;
-    for (int k = 0; k < L::D; ++k) same = same && (L::c(m, k) == -L::c(l, k));
-    if (same) return m;
-  }
-  return -1;
+  return L::opp(l);
 }
+
+// opp must send every direction to its negative (checked at compile time).
+template <class L>
+__host__ __device__ constexpr bool opp_is_negation() {
+  for (int l = 0; l < L::Q; ++l)
+    for (int k = 0; k < L::D; ++k)
+      if (L::c(L::opp(l), k) != -L::c(l, k)) return false;
+  return true;
+}
+static_assert(opp_is_negation<Lattice<0>>(), "D2Q9 opposite table");
+static_assert(opp_is_negation<Lattice<1>>(), "D3Q19 opposite table");
+static_assert(opp_is_negation<Lattice<2>>(), "D3Q27 opposite table");
 
 // Packed symmetric-tensor component t -> axis pair (a, b), a <= b
 template <class L>

@@ -118,6 +118,91 @@ __device__ __forceinline__ void kbc(const T (&f)[L::Q], const T (&feq)[L::Q], T 
   for (int l = 0; l < L::Q; ++l) fo[l] = f[l] - beta * (two * ds[l] + gamma * dh[l]);
 }
 
+// BGK in pair form (collision code 2): the same equations as macroscopic +
+// quadratic equilibrium + BGK, arranged over opposite-direction pairs (l, opp l)
+// with l < opp l.  rho and j come from the pair sums and differences, u = j / rho
+// uses one reciprocal, feq of a pair shares e = 1 - 1.5|u|^2 + 4.5 (c.u)^2 and
+// t = 3 c.u, and the update is f_out = (1 - omega) f + (omega rho w) (e +- t).
+// About 190 floating-point operations per D3Q19 cell instead of about 325;
+// results differ from XLB's operation order by rounding only.
+template <class L>
+__host__ __device__ constexpr bool pair_lead(int l) {
+  return l != 0 && l < opp<L>(l);
+}
+
+// The p-th pair lead (pairs ordered by increasing l).
+template <class L>
+__host__ __device__ constexpr int pair_at(int p) {
+  int k = 0;
+  for (int l = 1; l < L::Q; ++l) {
+    if (pair_lead<L>(l)) {
+      if (k == p) return l;
+      ++k;
+    }
+  }
+  return -1;
+}
+
+// Recursion over pairs so every index is a compile-time constant.
+template <class L, class T, int P>
+__device__ __forceinline__ void pair_moments(const T (&f)[L::Q], T& rho, T (&j)[L::D]) {
+  if constexpr (P < (L::Q - 1) / 2) {
+    constexpr int l = pair_at<L>(P);
+    constexpr int o = opp<L>(l);
+    const T sig = f[l] + f[o];
+    const T dif = f[l] - f[o];
+    rho = rho + sig;
+#pragma unroll
+    for (int d = 0; d < L::D; ++d) {
+      if (L::c(l, d) == 1) j[d] = j[d] + dif;
+      if (L::c(l, d) == -1) j[d] = j[d] - dif;
+    }
+    pair_moments<L, T, P + 1>(f, rho, j);
+  }
+}
+
+template <class L, class T, int P>
+__device__ __forceinline__ void pair_update(const T (&f)[L::Q], const T (&u)[L::D], T base, T omf, T orho,
+                                            T (&fo)[L::Q]) {
+  if constexpr (P < (L::Q - 1) / 2) {
+    constexpr int l = pair_at<L>(P);
+    constexpr int o = opp<L>(l);
+    T cu = T(0);
+#pragma unroll
+    for (int d = 0; d < L::D; ++d) {
+      if (L::c(l, d) == 1) cu = cu + u[d];
+      if (L::c(l, d) == -1) cu = cu - u[d];
+    }
+    const T e = base + T(4.5) * (cu * cu);
+    const T t = T(3) * cu;
+    const T ow = orho * T(weight<L>(l));
+    fo[l] = omf * f[l] + ow * (e + t);
+    fo[o] = omf * f[o] + ow * (e - t);
+    pair_update<L, T, P + 1>(f, u, base, omf, orho, fo);
+  }
+}
+
+template <class L, class T>
+__device__ __forceinline__ void bgk_pair(const T (&f)[L::Q], T omega, T (&fo)[L::Q]) {
+  T rho = f[0];
+  T j[L::D];
+#pragma unroll
+  for (int d = 0; d < L::D; ++d) j[d] = T(0);
+  pair_moments<L, T, 0>(f, rho, j);
+  const T inv = T(1) / rho;
+  T u[L::D];
+#pragma unroll
+  for (int d = 0; d < L::D; ++d) u[d] = j[d] * inv;
+  T usq = u[0] * u[0];
+#pragma unroll
+  for (int d = 1; d < L::D; ++d) usq = usq + u[d] * u[d];
+  const T base = T(1) - T(1.5) * usq;
+  const T omf = T(1) - omega;
+  const T orho = omega * rho;
+  fo[0] = omf * f[0] + orho * T(weight<L>(0)) * base;
+  pair_update<L, T, 0>(f, u, base, omf, orho, fo);
+}
+
 // -c of the first missing direction with |c|_1 = 1 (helper_functions_bc.py:250-261,
 // bc_extrapolation_outflow.py:358-369).  Zero when there is none.
 template <class L>

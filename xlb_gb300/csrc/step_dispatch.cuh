@@ -41,10 +41,49 @@ int launch_step_t(const StepArgs& a, int sk, int compute, bool fullbc, bool diag
   return (int)cudaGetLastError();
 }
 
-int launch_step_d2q9_bgk(const StepArgs&, int, int, bool, bool, cudaStream_t);
+// Marching kernel; `threads` per block (multiple of 32), `chunk` rows of axis 1 per thread.
+template <int LAT, int COLL>
+int launch_step_march_t(const StepArgs& a, int sk, int compute, bool fullbc, int threads, int chunk, cudaStream_t s) {
+  using L = Lattice<LAT>;
+  const int zblocks = (a.n2 + threads - 1) / threads;
+  const dim3 grid((unsigned)(a.n0 * zblocks), (unsigned)((a.n1 + chunk - 1) / chunk));
+#define XLBG_MLAUNCH(SKV, TV)                                                                  \
+  do {                                                                                       \
+    if (fullbc)                                                                              \
+      step_kernel_march<L, SKV, TV, COLL, true><<<grid, threads, 0, s>>>(a, chunk);         \
+    else                                                                                     \
+      step_kernel_march<L, SKV, TV, COLL, false><<<grid, threads, 0, s>>>(a, chunk);        \
+  } while (0)
+  if (compute == 1) {
+    switch (sk) {
+      case SK_F64: XLBG_MLAUNCH(SK_F64, double); break;
+      case SK_F32: XLBG_MLAUNCH(SK_F32, double); break;
+      case SK_F16: XLBG_MLAUNCH(SK_F16, double); break;
+      default: return -1;
+    }
+  } else {
+    switch (sk) {
+      case SK_F32: XLBG_MLAUNCH(SK_F32, float); break;
+      case SK_F16: XLBG_MLAUNCH(SK_F16, float); break;
+      case SK_F16S: XLBG_MLAUNCH(SK_F16S, float); break;
+      case SK_BF16S: XLBG_MLAUNCH(SK_BF16S, float); break;
+      default: return -1;
+    }
+  }
+#undef XLBG_MLAUNCH
+  return (int)cudaGetLastError();
+}
+
+int launch_step_march_d2q9_bgk(const StepArgs&, int, int, bool, bool, int, int, cudaStream_t);
+int launch_step_march_d2q9_kbc(const StepArgs&, int, int, bool, int, int, cudaStream_t);
+int launch_step_march_d3q19_bgk(const StepArgs&, int, int, bool, bool, int, int, cudaStream_t);
+int launch_step_march_d3q27_bgk(const StepArgs&, int, int, bool, bool, int, int, cudaStream_t);
+int launch_step_march_d3q27_kbc(const StepArgs&, int, int, bool, int, int, cudaStream_t);
+
+int launch_step_d2q9_bgk(const StepArgs&, int, int, bool, bool, bool, cudaStream_t);
 int launch_step_d2q9_kbc(const StepArgs&, int, int, bool, bool, cudaStream_t);
-int launch_step_d3q19_bgk(const StepArgs&, int, int, bool, bool, cudaStream_t);
-int launch_step_d3q27_bgk(const StepArgs&, int, int, bool, bool, cudaStream_t);
+int launch_step_d3q19_bgk(const StepArgs&, int, int, bool, bool, bool, cudaStream_t);
+int launch_step_d3q27_bgk(const StepArgs&, int, int, bool, bool, bool, cudaStream_t);
 int launch_step_d3q27_kbc(const StepArgs&, int, int, bool, bool, cudaStream_t);
 
 }  // namespace xlbg

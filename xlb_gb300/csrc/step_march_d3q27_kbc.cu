@@ -1,0 +1,8 @@
+// Marching step kernels for D3Q27 with KBC collision.
+#include "step_dispatch.cuh"
+
+namespace xlbg {
+int launch_step_march_d3q27_kbc(const StepArgs& a, int sk, int compute, bool fullbc, int threads, int chunk, cudaStream_t s) {
+  return launch_step_march_t<2, 1>(a, sk, compute, fullbc, threads, chunk, s);
+}
+}  // namespace xlbg

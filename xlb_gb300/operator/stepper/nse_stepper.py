@@ -56,13 +56,17 @@ class IncompressibleNavierStokesStepper(Stepper):
     ):
         super().__init__(grid, boundary_conditions)
         if collision_type == "BGK":
-            self.collision_code = _lib.BGK
+            # The shifted FP16/BF16 forms have no XLB counterpart and use BGK in pair
+            # form (same equations, fewer operations); the others keep XLB's order.
+            self.collision_code = _lib.BGK_PAIR if self.precision_policy.shifted else _lib.BGK
+        elif collision_type == "BGK_PAIR":
+            self.collision_code = _lib.BGK_PAIR
         elif collision_type == "KBC":
             if (self.velocity_set.d, self.velocity_set.q) == (3, 19):
                 raise NotImplementedError(f"Velocity set not supported for KBC: {self.velocity_set}")
             self.collision_code = _lib.KBC
         else:
-            raise NotImplementedError(f"collision_type {collision_type!r} is not on this path (BGK, KBC)")
+            raise NotImplementedError(f"collision_type {collision_type!r} is not on this path (BGK, BGK_PAIR, KBC)")
         if force_vector is not None:
             raise NotImplementedError("forced collision is not on this path")
         if streaming_scheme != "pull":
