@@ -306,7 +306,9 @@ static int launch_main(const xlbg_desc* d, const StepArgs& a, bool diag, cudaStr
   const bool full = needs_full_bc(d) || diag;
   const bool pair = d->collision == XLBG_BGK_PAIR;
   int r = -1;
-  if (!diag && a.ncell < 0x7fffffffLL) {
+  // the marching kernel indexes with 32-bit offsets: every plane offset l * cells + cell must fit
+  const long long q = d->lattice == 0 ? 9 : (d->lattice == 1 ? 19 : 27);
+  if (!diag && q * a.ncell <= 0xffffffffLL) {
     const int threads = a.n2 >= kStepBlock ? kStepBlock : ((a.n2 + 31) / 32) * 32;
     const int chunk = choose_chunk(a, threads);
     if (chunk > 0) {

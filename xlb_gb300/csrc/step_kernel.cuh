@@ -53,6 +53,19 @@ struct StepArgs {
   double* diag_slots;  // kDiagSlots x 4 doubles, zero on entry
 };
 
+// Element (l, i) of f0 / f1 in the store type.  Idx is the index type of the
+// whole plane-and-cell offset: long long in general, unsigned 32-bit in the
+// marching kernel, which runs only when Q * cells < 2^32 (the host checks) and
+// saves the 64-bit multiply per access.
+template <class Bits, class Idx>
+__device__ __forceinline__ const Bits* at0(const StepArgs& a, int l, Idx i) {
+  return static_cast<const Bits*>(a.f0) + ((Idx)l * (Idx)a.ncell + i);
+}
+template <class Bits, class Idx>
+__device__ __forceinline__ Bits* at1(const StepArgs& a, int l, Idx i) {
+  return static_cast<Bits*>(a.f1) + ((Idx)l * (Idx)a.ncell + i);
+}
+
 template <class T>
 __device__ __forceinline__ T omega_of(const StepArgs& a) {
   if constexpr (sizeof(T) == 4)
@@ -104,30 +117,64 @@ template <class L, int SK, class T>
 __device__ __forceinline__ void pull_cell(const StepArgs& a, int i0, int i1, int i2, T (&f)[L::Q]) {
   using St = Store<SK, T>;
   using Bits = typename St::Bits;
-  const Bits* __restrict__ f0 = static_cast<const Bits*>(a.f0);
-  const long long N = a.ncell;
   const int n2 = a.n2;
   const RowOffsets rows(i0, i1, a.n0, a.n1, n2);
   const int z[3] = {i2 == n2 - 1 ? 0 : i2 + 1, i2, i2 == 0 ? n2 - 1 : i2 - 1};  // source i2 for c2 = -1, 0, +1
 #pragma unroll
   for (int l = 0; l < L::Q; ++l) {
-    const Bits* p = f0 + (long long)l * N + rows.of<L>(l);
-    f[l] = St::dec(ldg_bits(p + z[axis_c<L>(l, 2) + 1]), T(weight<L>(l)));
+    f[l] = St::dec(ldg_bits(at0<Bits>(a, l, rows.of<L>(l) + z[axis_c<L>(l, 2) + 1])), T(weight<L>(l)));
   }
+}
+
+// Collision of one cell: XLB-order BGK (COLL 0), KBC (COLL 1) or pair-form BGK (COLL 2).
+template <class L, class T, int COLL>
+__device__ __forceinline__ void collide(const T (&f)[L::Q], T omega, T (&fo)[L::Q]) {
+  if constexpr (COLL == 2) {
+    bgk_pair<L>(f, omega, fo);
+  } else {
+    T rho, u[L::D];
+    macroscopic<L>(f, rho, u);
+    T feq[L::Q];
+    equilibrium<L>(rho, u, feq);
+    if constexpr (COLL == 0) {
+#pragma unroll
+      for (int l = 0; l < L::Q; ++l) fo[l] = f[l] - omega * (f[l] - feq[l]);
+    } else {
+      kbc<L>(f, feq, rho, omega, fo);
+    }
+  }
+}
+
+// Store of one cell's post-collision populations (nse_stepper.py:379-381); with
+// DIAG, the cell's mass as stored, summed in T.
+template <class L, int SK, class T, bool DIAG, class Idx>
+__device__ __forceinline__ void store_cell(const StepArgs& a, Idx cell, const T (&fo)[L::Q], double& dmass) {
+  using St = Store<SK, T>;
+  using Bits = typename St::Bits;
+  T msum = T(0);
+#pragma unroll
+  for (int l = 0; l < L::Q; ++l) {
+    const Bits b = St::enc(fo[l], T(weight<L>(l)));
+    *at1<Bits>(a, l, cell) = b;
+    if constexpr (DIAG) {
+      const T v = St::dec(b, T(weight<L>(l)));
+      msum = l == 0 ? v : msum + v;
+    }
+  }
+  if constexpr (DIAG) dmass = (double)msum;
 }
 
 // Everything after the pull for one cell: BC lookup, streaming-step BC,
 // collision, collision-step BC, store to f1 and the diagnostics contributions.
 // f holds the pulled values of the cell; the cell is not a skip cell (id 255).
-template <class L, int SK, class T, int COLL, bool FULLBC, bool DIAG>
-__device__ __forceinline__ void cell_update(const StepArgs& a, int i0, int i1, int i2, long long cell, uint8_t id,
+// The collision is inlined once, shared by fluid and boundary cells (a second
+// copy for a fluid-only path doubled the code and ran slower).
+template <class L, int SK, class T, int COLL, bool FULLBC, bool DIAG, class Idx>
+__device__ __forceinline__ void cell_update(const StepArgs& a, int i0, int i1, int i2, Idx cell, uint8_t id,
                                             T (&f)[L::Q], double& dmass, double (&dforce)[3]) {
   using St = Store<SK, T>;
   using Bits = typename St::Bits;
   constexpr int Q = L::Q;
-  const Bits* __restrict__ f0 = static_cast<const Bits*>(a.f0);
-  Bits* __restrict__ f1 = static_cast<Bits*>(a.f1);
-  const long long N = a.ncell;
   const int n1 = a.n1, n2 = a.n2;
   // ---- boundary lookup (XLB unrolls the BC list the same way, nse_stepper.py:280-293) ----
   int kind = 0;
@@ -154,7 +201,7 @@ __device__ __forceinline__ void cell_update(const StepArgs& a, int i0, int i1, i
 #pragma unroll
       for (int l = 0; l < Q; ++l) {
         if ((miss >> l) & 1u)
-          f[l] = St::dec(ldg_bits(f0 + (long long)opp<L>(l) * N + cell), T(weight<L>(opp<L>(l))));
+          f[l] = St::dec(ldg_bits(at0<Bits>(a, opp<L>(l), cell)), T(weight<L>(opp<L>(l))));
       }
     } else if (kind == BC_EQUILIBRIUM) {
       // bc_equilibrium.py:255-271
@@ -164,28 +211,14 @@ __device__ __forceinline__ void cell_update(const StepArgs& a, int i0, int i1, i
       equilibrium<L>(T(bc_rho), u, f);
     } else if (FULLBC && kind >= BC_ZOUHE_V && kind <= BC_REG_P) {
       // the prescribed value lives in slot 0 of f1 (boundary_condition.py:151-152)
-      const T aux = St::dec_raw(ldg_bits(f1 + cell));
+      const T aux = St::dec_raw(*at1<Bits>(a, 0, cell));
       zouhe_like<L>(f, miss, aux, kind);
     }
   }
 
   // ---- macroscopic, equilibrium, collision ----
-  const T omega = omega_of<T>(a);
   T fo[Q];
-  if constexpr (COLL == 2) {
-    bgk_pair<L>(f, omega, fo);
-  } else {
-    T rho, u[L::D];
-    macroscopic<L>(f, rho, u);
-    T feq[Q];
-    equilibrium<L>(rho, u, feq);
-    if constexpr (COLL == 0) {
-#pragma unroll
-      for (int l = 0; l < Q; ++l) fo[l] = f[l] - omega * (f[l] - feq[l]);
-    } else {
-      kbc<L>(f, feq, rho, omega, fo);
-    }
-  }
+  collide<L, T, COLL>(f, omega_of<T>(a), fo);
 
   // ---- collision-step BCs ----
   if (kind == BC_FULLWAY) {
@@ -209,26 +242,14 @@ __device__ __forceinline__ void cell_update(const StepArgs& a, int i0, int i1, i
         const int s1 = wrap_any(i1 - (axis_c<L>(l, 1) + m1), n1);
         const int s2 = wrap_any(i2 - (axis_c<L>(l, 2) + m2), n2);
         const long long src = ((long long)s0 * n1 + s1) * n2 + s2;
-        const T faux = St::dec(ldg_bits(f0 + (long long)l * N + src), T(weight<L>(l)));
+        const T faux = St::dec(ldg_bits(at0<Bits>(a, l, (Idx)src)), T(weight<L>(l)));
         fo[opp<L>(l)] = (T(1) - cs) * f[l] + cs * faux;
       }
     }
   }
 
-  // ---- store ----
-  T msum = T(0);
-#pragma unroll
-  for (int l = 0; l < Q; ++l) {
-    const Bits b = St::enc(fo[l], T(weight<L>(l)));
-    f1[(long long)l * N + cell] = b;
-    if constexpr (DIAG) {
-      // mass of the stored state, summed per cell in T
-      const T v = St::dec(b, T(weight<L>(l)));
-      msum = l == 0 ? v : msum + v;
-    }
-  }
+  store_cell<L, SK, T, DIAG>(a, cell, fo, dmass);
   if constexpr (DIAG) {
-    dmass = (double)msum;
     if ((int)id == a.force_id && !(miss & 1u)) {
       // momentum exchange on the input state (momentum_transfer.py:130-158):
       // phi_l = f0[opp l] + f_post_stream[l] with f_post_stream[l] = f0[opp l]
@@ -238,7 +259,7 @@ __device__ __forceinline__ void cell_update(const StepArgs& a, int i0, int i1, i
 #pragma unroll
       for (int l = 0; l < Q; ++l) {
         if ((miss >> l) & 1u) {
-          const T v = St::dec(ldg_bits(f0 + (long long)opp<L>(l) * N + cell), T(weight<L>(opp<L>(l))));
+          const T v = St::dec(ldg_bits(at0<Bits>(a, opp<L>(l), cell)), T(weight<L>(opp<L>(l))));
           const T phi = v + v;
 #pragma unroll
           for (int d = 0; d < L::D; ++d) {
@@ -334,8 +355,7 @@ __global__ void __launch_bounds__(kStepBlock, march_min_blocks<L, T>()) step_ker
   using Bits = typename St::Bits;
   constexpr int Q = L::Q;
 
-  const Bits* __restrict__ f0 = static_cast<const Bits*>(a.f0);
-  const long long N = a.ncell;  // < 2^31 here (the host checks), so cell indices are 32-bit
+  // Q * cells < 2^32 here (the host checks), so every offset is 32-bit
   const int n0 = a.n0, n1 = a.n1, n2 = a.n2;
   const int zblocks = (n2 + blockDim.x - 1) / blockDim.x;
   const int i0 = blockIdx.x / zblocks;
@@ -364,9 +384,9 @@ __global__ void __launch_bounds__(kStepBlock, march_min_blocks<L, T>()) step_ker
 #pragma unroll
     for (int l = 0; l < Q; ++l) {
       const unsigned src = xz[axis_c<L>(l, 0) + 1][axis_c<L>(l, 2) + 1] + yo[axis_c<L>(l, 1) + 1];
-      f[l] = St::dec(ldg_bits(f0 + l * N + src), T(weight<L>(l)));
+      f[l] = St::dec(ldg_bits(at0<Bits>(a, l, src)), T(weight<L>(l)));
     }
-    cell_update<L, SK, T, COLL, FULLBC, false>(a, i0, i1, i2, (long long)cell, id, f, dm, df);
+    cell_update<L, SK, T, COLL, FULLBC, false>(a, i0, i1, i2, cell, id, f, dm, df);
   }
 }
 
