@@ -170,6 +170,50 @@ int xlbg_step_diag_noalloc(const xlbg_desc* desc, void* f0, void* f1, const uint
                            int32_t timestep, int32_t force_id, double* diag, void* stream);
 
 /*
+ * Differentiation.  XLB differentiates its stepper by taping Warp kernels
+ * (examples/out_of_core/subroutine/autodiff_stepper_subroutine.py:460-466,
+ * segments of examples/out_of_core/autodiff_lbm.py:64-124); these two entry
+ * points replace the tape with a recorded segment of states and a hand-written
+ * adjoint kernel.  The state of a step is the population field alone: the
+ * ZouHe / Regularized prescribed values, which XLB carries from step to step in
+ * f_1 slot 0 (nse_stepper.py:318-342), are passed as a separate field aux (one
+ * store-type value per cell, read at those BC cells only; NULL allowed when the
+ * BC list has no ZouHe / Regularized BC).
+ *
+ * xlbg_forward_segment: states holds n_steps + 1 consecutive population fields
+ * of Q * cells store elements; for j = 0 .. n_steps - 1 it writes state j + 1 =
+ * one step of state j, with the results of xlbg_step when f_1 slot 0 holds aux.
+ * No aux recovery: state j is not modified.
+ */
+int xlbg_forward_segment(const xlbg_desc* desc, void* states, int32_t n_steps, const uint8_t* bc_mask,
+                         const uint32_t* miss_bits, const void* aux, double omega, void* stream);
+
+/*
+ * xlbg_adjoint_segment: the reverse sweep over a recorded segment.  states
+ * holds the n_steps input states of the segment's steps (state j is the input
+ * of step j, as written by xlbg_forward_segment).  lam_a holds dL/d(state after
+ * the last step) on entry; the sweep ping-pongs between lam_a and lam_b and
+ * leaves dL/d(state 0) in lam_a when n_steps is even, in lam_b when it is odd.
+ * lam_a / lam_b are Q planes of the compute type.
+ *
+ * bc_cells / n_bc: sorted linear indices of every cell whose bc id is a
+ * HalfwayBounceBack, ExtrapolationOutflow, ZouHe or Regularized BC (the cells
+ * whose step reads own-cell or neighbour values besides the pull, or aux).
+ * aux_grad: n_bc compute-type values; at the ZouHe / Regularized cells of the
+ * list, dL/d(aux of that cell) summed over the segment's steps is added to it.
+ *
+ * Supported: FP32 store with FP32 or FP64 compute, FP64 store with FP64
+ * compute; BGK (XLBG_BGK and XLBG_BGK_PAIR, same equations) and KBC; every BC
+ * kind.  bc_mask must not contain id 255.  Each step is two kernels: every cell
+ * pushes the adjoint of its pulled values back along -c (plain stores; the pull
+ * is a bijection per direction), then the listed cells add their own-cell,
+ * neighbour and aux terms atomically.  Replaces the tape's backward pass.
+ */
+int xlbg_adjoint_segment(const xlbg_desc* desc, const void* states, int32_t n_steps, const uint8_t* bc_mask,
+                         const uint32_t* miss_bits, const void* aux, const int64_t* bc_cells, int64_t n_bc,
+                         void* lam_a, void* lam_b, void* aux_grad, double omega, void* stream);
+
+/*
  * f = feq(rho, u) in the store form for every cell (initializers.py:5-20 with
  * quadratic_equilibrium.py:63-82).  rho: (1, cells) and u: (d, cells) in the
  * compute type, or NULL for the uniform values rho0 / u0[d].

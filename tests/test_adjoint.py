@@ -1,0 +1,182 @@
+"""Differentiation: the hand-written adjoint against torch autograd through the
+FP64 torch restatement (oracle/lbm_torch.py) and against FP64 central finite
+differences.
+
+XLB's own gradient comes from Warp's tape or jax.grad, neither of which runs
+here; torch autograd of an FP64 restatement of the same step stands in for
+them, and is itself pinned to the numpy oracle's forward step and to finite
+differences by the CPU tests below.
+
+Loss used throughout: L = sum(W * f_K) with a fixed random W, so dL/df_K = W
+and the tests check the full vector-Jacobian product of K steps.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+from _scenarios import Scenario
+from oracle import lbm_oracle as O
+from oracle import lbm_torch as TO
+
+# (lattice, shape, layout, collision)
+CASES = [
+    ("D2Q9", (14, 10), "cavity_fullway", "BGK"),
+    ("D2Q9", (14, 10), "cavity_halfway", "BGK"),
+    ("D2Q9", (16, 10), "channel_zouhe", "BGK"),
+    ("D2Q9", (16, 10), "channel_regularized", "BGK"),
+    ("D2Q9", (16, 10), "channel_pressure", "KBC"),
+    ("D2Q9", (12, 8), "periodic", "KBC"),
+    ("D3Q19", (10, 8, 6), "channel_zouhe", "BGK"),
+    ("D3Q19", (10, 8, 6), "channel_regularized", "BGK"),
+    ("D3Q19", (8, 8, 8), "cavity_fullway", "BGK"),
+    ("D3Q27", (10, 8, 6), "channel_regularized", "KBC"),
+    ("D3Q27", (10, 8, 6), "channel_pressure", "BGK"),
+]
+
+
+def _oracle_setup(lattice, shape, layout, collision, seed=3):
+    sc = Scenario(lattice, shape, layout, "fp64", collision, omega=1.6)
+    sc.randomize(seed)
+    aux = TO.aux_field(sc.lat, sc.f0.shape[1:], sc.bc_mask, sc.f1[0], sc.obcs)
+    return sc, aux
+
+
+def _torch_grad(sc, aux, steps, W):
+    f = torch.from_numpy(sc.f0.copy()).requires_grad_(True)
+    a = torch.from_numpy(aux.copy()).requires_grad_(True)
+    out = TO.run(sc.lat, f, a, sc.bc_mask, sc.missing, sc.omega, sc.obcs, steps, sc.collision)
+    (out * torch.from_numpy(W)).sum().backward()
+    return f.grad.numpy(), (a.grad.numpy() if a.grad is not None else np.zeros_like(aux))
+
+
+# ---------------------------------------------------------------------------- CPU: the oracle itself
+
+
+@pytest.mark.parametrize("case", CASES[:4] + CASES[6:7] + CASES[9:10], ids=lambda c: f"{c[0]}-{c[2]}-{c[3]}")
+def test_torch_restatement_matches_numpy_oracle(case):
+    sc, aux = _oracle_setup(*case)
+    f_np, _ = sc.oracle_steps(3)
+    f_t = TO.run(sc.lat, torch.from_numpy(sc.f0.copy()), torch.from_numpy(aux), sc.bc_mask, sc.missing, sc.omega,
+                 sc.obcs, 3, sc.collision)
+    np.testing.assert_allclose(f_t.numpy(), f_np, rtol=0, atol=1e-15)
+
+
+@pytest.mark.parametrize("case", [CASES[2], CASES[3], CASES[4]], ids=lambda c: f"{c[0]}-{c[2]}-{c[3]}")
+def test_torch_gradient_matches_finite_differences(case):
+    """Directional derivative of L along random directions of f_init and aux."""
+    sc, aux = _oracle_setup(*case)
+    steps = 3
+    rng = np.random.default_rng(11)
+    W = rng.standard_normal(sc.f0.shape)
+    gf, ga = _torch_grad(sc, aux, steps, W)
+
+    def loss(f0, a):
+        out = TO.run(sc.lat, torch.from_numpy(f0), torch.from_numpy(a), sc.bc_mask, sc.missing, sc.omega, sc.obcs,
+                     steps, sc.collision)
+        return float((out * torch.from_numpy(W)).sum())
+
+    h = 1e-6
+    vf = rng.standard_normal(sc.f0.shape) * 1e-2
+    fd = (loss(sc.f0 + h * vf, aux) - loss(sc.f0 - h * vf, aux)) / (2 * h)
+    assert abs(fd - np.sum(gf * vf)) <= 1e-6 * max(1.0, abs(fd))
+    aux_mask = aux != 0
+    if aux_mask.any():
+        va = rng.standard_normal(aux.shape) * 1e-2 * aux_mask
+        fd = (loss(sc.f0, aux + h * va) - loss(sc.f0, aux - h * va)) / (2 * h)
+        assert abs(fd - np.sum(ga * va)) <= 1e-6 * max(1.0, abs(fd))
+
+
+# ---------------------------------------------------------------------------- GPU: the adjoint kernel
+
+
+def _gpu_grad(sc, steps, W, checkpoint_every, policy_dtype=torch.float64):
+    f_0, f_1, bcm, mm = sc.gpu_fields()
+    run = sc.stepper.differentiable(bcm, mm, sc.omega, steps, checkpoint_every=checkpoint_every)
+    f = f_0.clone().requires_grad_(True)
+    a = run.aux_from_fields(f_1).clone().requires_grad_(True)
+    out = run(f, a)
+    (out.double() * torch.from_numpy(W).cuda()).sum().backward()
+    ga_full = np.zeros(sc.f0.shape[1:], dtype=np.float64)
+    if a.grad is not None:
+        ga_full.reshape(-1)[run.aux_cells.cpu().numpy()] = a.grad.double().cpu().numpy()
+    return out.detach().double().cpu().numpy(), f.grad.double().cpu().numpy(), ga_full
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", CASES, ids=lambda c: f"{c[0]}-{c[2]}-{c[3]}")
+def test_adjoint_fp64_matches_autograd(case):
+    steps = 5
+    sc, aux = _oracle_setup(*case)
+    W = np.random.default_rng(5).standard_normal(sc.f0.shape)
+    gf_ref, ga_ref = _torch_grad(sc, aux, steps, W)
+    out, gf, ga = _gpu_grad(sc, steps, W, checkpoint_every=2)
+    f_ref, _ = sc.oracle_steps(steps)
+    np.testing.assert_array_equal(out, f_ref)  # the recorded forward is the exact step
+    assert _rel(gf, gf_ref) < 1e-12
+    if np.any(ga_ref):
+        assert _rel(ga, ga_ref) < 1e-12
+
+
+@pytest.mark.gpu
+def test_adjoint_checkpoint_schedule_is_exact():
+    """Any checkpoint spacing replays the same states, so gradients agree bit for bit."""
+    sc, _ = _oracle_setup("D2Q9", (16, 10), "channel_zouhe", "BGK")
+    W = np.random.default_rng(6).standard_normal(sc.f0.shape)
+    ref = _gpu_grad(sc, 7, W, checkpoint_every=7)
+    for k in (1, 2, 3):
+        got = _gpu_grad(sc, 7, W, checkpoint_every=k)
+        np.testing.assert_array_equal(got[1], ref[1])
+        np.testing.assert_array_equal(got[2], ref[2])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", [CASES[2], CASES[7], CASES[9]], ids=lambda c: f"{c[0]}-{c[2]}-{c[3]}")
+def test_adjoint_fp64_matches_finite_differences(case):
+    """GPU adjoint against FP64 central differences of the GPU forward."""
+    steps = 6
+    sc, _ = _oracle_setup(*case)
+    rng = np.random.default_rng(8)
+    W = rng.standard_normal(sc.f0.shape)
+    _, gf, _ = _gpu_grad(sc, steps, W, checkpoint_every=4)
+    f_0, f_1, bcm, mm = sc.gpu_fields()
+    run = sc.stepper.differentiable(bcm, mm, sc.omega, steps, checkpoint_every=steps)
+    a = run.aux_from_fields(f_1)
+    Wt = torch.from_numpy(W).cuda()
+    v = torch.from_numpy(rng.standard_normal(sc.f0.shape) * 1e-2).cuda()
+    h = 1e-6
+    with torch.no_grad():
+        lp = float((run(f_0 + h * v, a) * Wt).sum())
+        lm = float((run(f_0 - h * v, a) * Wt).sum())
+    fd = (lp - lm) / (2 * h)
+    assert abs(fd - float(np.sum(gf * v.cpu().numpy()))) <= 1e-6 * max(1.0, abs(fd))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", [CASES[2], CASES[3], CASES[6], CASES[9]], ids=lambda c: f"{c[0]}-{c[2]}-{c[3]}")
+def test_adjoint_fp32_close_to_fp64(case):
+    """FP32FP32 adjoint against the FP64 gradient of the same set-up (FP32 rounding only)."""
+    steps = 5
+    sc64, aux = _oracle_setup(*case)
+    W = np.random.default_rng(9).standard_normal(sc64.f0.shape)
+    gf_ref, ga_ref = _torch_grad(sc64, aux, steps, W)
+    sc32 = Scenario(case[0], case[1], case[2], "fp32", case[3], omega=1.6)
+    sc32.f0 = sc64.f0.astype(np.float32)
+    sc32.f1 = O.aux_init(sc32.lat, sc32.store, sc32.f0.copy(), sc32.bc_mask, sc32.missing, sc32.obcs, np.float32)
+    _, gf, ga = _gpu_grad(sc32, steps, W, checkpoint_every=2)
+    assert _rel(gf, gf_ref) < 1e-4
+    if np.any(ga_ref):
+        assert _rel(ga, ga_ref) < 1e-3
+
+
+@pytest.mark.gpu
+def test_adjoint_rejects_skip_cells():
+    sc, _ = _oracle_setup("D2Q9", (12, 8), "cavity_fullway", "BGK")
+    f_0, f_1, bcm, mm = sc.gpu_fields()
+    bcm[0, 5, 4, 0] = 255
+    with pytest.raises(NotImplementedError):
+        sc.stepper.differentiable(bcm, mm, sc.omega, 3)

@@ -39,6 +39,8 @@ EXPORTED = (
     "xlbg_run",
     "xlbg_step_diag",
     "xlbg_step_diag_noalloc",
+    "xlbg_forward_segment",
+    "xlbg_adjoint_segment",
     "xlbg_equilibrium",
     "xlbg_macroscopic",
 )
@@ -89,6 +91,8 @@ _SIGNATURES = {
     "xlbg_run": ([_DESC, _P, _P, _P, _P, _P, _I64, _P, _D, _I32, _I32, _P], ctypes.c_int),
     "xlbg_step_diag": ([_DESC, _P, _P, _P, _P, _P, _I64, _P, _D, _I32, _I32, _P, _P, _P], ctypes.c_int),
     "xlbg_step_diag_noalloc": ([_DESC, _P, _P, _P, _P, _P, _I64, _D, _I32, _I32, _P, _P], ctypes.c_int),
+    "xlbg_forward_segment": ([_DESC, _P, _I32, _P, _P, _P, _D, _P], ctypes.c_int),
+    "xlbg_adjoint_segment": ([_DESC, _P, _I32, _P, _P, _P, _P, _I64, _P, _P, _P, _D, _P], ctypes.c_int),
     "xlbg_equilibrium": ([_DESC, _P, _P, _D, ctypes.POINTER(_D), _P, _P], ctypes.c_int),
     "xlbg_macroscopic": ([_DESC, _P, _P, _P, _P], ctypes.c_int),
 }

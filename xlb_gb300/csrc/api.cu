@@ -252,10 +252,11 @@ static void recovery_pass(const xlbg_desc* d, bool save, void* f, const int64_t*
     recovery_by_size<Lattice<2>>(bytes, save, f, cells, miss, scratch, nrec, n, s);
 }
 
-static int fill_step_args(const xlbg_desc* d, const void* f0, void* f1, const uint8_t* bc_mask,
+int fill_step_args(const xlbg_desc* d, const void* f0, void* f1, const uint8_t* bc_mask,
                           const uint32_t* miss, double omega, StepArgs& a) {
   a.f0 = f0;
   a.f1 = f1;
+  a.aux = f1;
   a.bc_mask = bc_mask;
   a.miss = miss;
   a.ncell = ncells(d);
@@ -302,7 +303,7 @@ static int choose_chunk(const StepArgs& a, int threads) {
   return (int)chunk;
 }
 
-static int launch_main(const xlbg_desc* d, const StepArgs& a, bool diag, cudaStream_t s) {
+int launch_main(const xlbg_desc* d, const StepArgs& a, bool diag, cudaStream_t s) {
   const bool full = needs_full_bc(d) || diag;
   const bool pair = d->collision == XLBG_BGK_PAIR;
   int r = -1;

@@ -42,6 +42,10 @@ struct StepArgs {
   void* f1;
   const uint8_t* bc_mask;
   const uint32_t* miss;
+  // one store-type value per cell holding the ZouHe / Regularized prescribed
+  // values: plane 0 of f1 in XLB's encoding (boundary_condition.py:151-152),
+  // or a separate field for the recording and adjoint entry points
+  const void* aux;
   long long ncell;
   int n0, n1, n2;
   int nbc;
@@ -211,7 +215,7 @@ __device__ __forceinline__ void cell_update(const StepArgs& a, int i0, int i1, i
       equilibrium<L>(T(bc_rho), u, f);
     } else if (FULLBC && kind >= BC_ZOUHE_V && kind <= BC_REG_P) {
       // the prescribed value lives in slot 0 of f1 (boundary_condition.py:151-152)
-      const T aux = St::dec_raw(*at1<Bits>(a, 0, cell));
+      const T aux = St::dec_raw(static_cast<const Bits*>(a.aux)[cell]);
       zouhe_like<L>(f, miss, aux, kind);
     }
   }
