@@ -41,6 +41,7 @@ def parse():
     p.add_argument("--no-forms", action="store_true", help="skip the FP16/BF16 store-form lines")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint/forward measurement")
     return p.parse_args()
 
 
@@ -345,6 +346,11 @@ def main():
             "d2h_bytes_per_step": d2h / args.steps,
             "what": "public stepper(...) call per step with caller swap; initial populations+masks H2D from pinned host and final populations D2H inside the timed region",
         }
+    if not args.no_adjoint and rank == 0:
+        # differentiation: D3Q19 128^3 channel, T=500, checkpoints every 100
+        import bench_adjoint
+
+        out["adjoint"] = bench_adjoint.measure(dim=3)
     if not args.no_cpu and rank == 0:
         out["cpu_baseline"] = cpu_baseline_sample()
     if rank == 0:

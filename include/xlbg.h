@@ -196,18 +196,18 @@ int xlbg_forward_segment(const xlbg_desc* desc, void* states, int32_t n_steps, c
  * leaves dL/d(state 0) in lam_a when n_steps is even, in lam_b when it is odd.
  * lam_a / lam_b are Q planes of the compute type.
  *
- * bc_cells / n_bc: sorted linear indices of every cell whose bc id is a
- * HalfwayBounceBack, ExtrapolationOutflow, ZouHe or Regularized BC (the cells
- * whose step reads own-cell or neighbour values besides the pull, or aux).
+ * bc_cells / n_bc: sorted linear indices of every cell with a non-zero bc id.
  * aux_grad: n_bc compute-type values; at the ZouHe / Regularized cells of the
  * list, dL/d(aux of that cell) summed over the segment's steps is added to it.
  *
  * Supported: FP32 store with FP32 or FP64 compute, FP64 store with FP64
  * compute; BGK (XLBG_BGK and XLBG_BGK_PAIR, same equations) and KBC; every BC
- * kind.  bc_mask must not contain id 255.  Each step is two kernels: every cell
- * pushes the adjoint of its pulled values back along -c (plain stores; the pull
- * is a bijection per direction), then the listed cells add their own-cell,
- * neighbour and aux terms atomically.  Replaces the tape's backward pass.
+ * kind.  bc_mask must not contain id 255.  Each step is two kernels: every
+ * fluid cell pushes the adjoint of its pulled values back along -c (plain
+ * stores; the pull is a bijection per direction) while boundary cells zero
+ * their push targets, then the listed boundary cells add their whole local
+ * adjoint (pushes, own-cell, neighbour and aux terms) atomically.  Replaces the
+ * tape's backward pass.
  */
 int xlbg_adjoint_segment(const xlbg_desc* desc, const void* states, int32_t n_steps, const uint8_t* bc_mask,
                          const uint32_t* miss_bits, const void* aux, const int64_t* bc_cells, int64_t n_bc,

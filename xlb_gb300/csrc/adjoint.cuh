@@ -10,11 +10,16 @@
 // (bc_zouhe.py:279-343, bc_regularized.py:134-202).  Given lam_out =
 // dL/df_{t+1}, the reverse step forms lam_in = dL/df_t as the sum over cells of
 // the transposed local Jacobians:
-//   pass 1, every cell: the P part, pushed to lam_in[l](y - c_l).  For each l
-//     the pull is a bijection of the cells, so every lam_in element is written
-//     exactly once, by a plain store: the reverse push-stream.
-//   pass 2, listed boundary cells only: the O and E parts, added atomically into
-//     lam_in after pass 1, and dL/da added to aux_grad.
+//   pass 1, every cell: a fluid cell pushes the P part to lam_in[l](y - c_l).
+//     For each l the pull is a bijection of the cells, so every lam_in element
+//     has exactly one pusher and takes a plain store: the reverse push-stream.
+//     A boundary cell stores zeros to its push targets instead.
+//   pass 2, the boundary cells (id != 0) only: the full local adjoint, whose P
+//     part is added atomically to the zeros of pass 1 and whose O and E parts
+//     are added atomically wherever they land; dL/da is added to aux_grad.
+//     Additions commute, so pass 2 needs no ordering among its threads.
+// Pass 1 thus runs the short fluid adjoint only (few registers, full
+// occupancy) and the boundary code runs on the surface cells alone.
 // Per cell the local Jacobian is applied in reverse program order:
 // collision-step BC, collision (BGK or KBC with the macroscopic and quadratic
 // equilibrium operators), streaming-step BC.  Each operator's adjoint below is
@@ -32,7 +37,7 @@ struct AdjArgs {
   StepArgs s;              // s.f0: forward input state f_t; s.aux: aux plane; s.f1 unused
   const void* lam_out;     // dL/df_{t+1}, compute type, Q planes
   void* lam_in;            // dL/df_t, compute type, Q planes
-  const long long* bc_cells;  // pass 2: sorted linear indices of the listed cells
+  const long long* bc_cells;  // pass 2: sorted linear indices of every cell with id != 0
   long long n_bc;
   void* aux_grad;          // pass 2: n_bc values, += dL/da at ZouHe / Regularized cells
 };
@@ -334,10 +339,10 @@ __device__ __forceinline__ void zouhe_adj(const T (&P)[L::Q], uint32_t miss, T a
   }
 }
 
-// Reverse of one cell.  g holds lam_out at the cell on entry; on return from
-// pass 1 it holds the adjoint of the pulled values P (to be pushed).  Pass 2
-// adds the own-cell, extrapolation-neighbour and aux terms instead.
-template <class L, int SK, class T, bool KBC, int PASS>
+// Reverse of one boundary cell.  g holds lam_out at the cell on entry and the
+// adjoint of the pulled values P on return (the caller pushes it); the
+// own-cell, extrapolation-neighbour and aux terms are added here, atomically.
+template <class L, int SK, class T, bool KBC>
 __device__ __forceinline__ void cell_adjoint(const AdjArgs& A, int i0, int i1, int i2, long long cell, uint8_t id,
                                              const T (&P)[L::Q], T (&g)[L::Q], long long list_index) {
   const StepArgs& a = A.s;
@@ -397,7 +402,7 @@ __device__ __forceinline__ void cell_adjoint(const AdjArgs& A, int i0, int i1, i
       if ((miss >> l) & 1u) {
         const T v = g[opp<L>(l)];
         ex[l] = (T(1) - cs) * v;
-        if constexpr (PASS == 2) {
+        {
           const int s0 = wrap_any(i0 - (axis_c<L>(l, 0) + m0), a.n0);
           const int s1 = wrap_any(i1 - (axis_c<L>(l, 1) + m1), a.n1);
           const int s2 = wrap_any(i2 - (axis_c<L>(l, 2) + m2), a.n2);
@@ -420,7 +425,7 @@ __device__ __forceinline__ void cell_adjoint(const AdjArgs& A, int i0, int i1, i
 #pragma unroll
     for (int l = 0; l < Q; ++l) {
       if ((miss >> l) & 1u) {
-        if constexpr (PASS == 2) atomicAdd(lam_in + (long long)opp<L>(l) * N + cell, fb[l]);
+        atomicAdd(lam_in + (long long)opp<L>(l) * N + cell, fb[l]);
         g[l] = T(0);
       } else {
         g[l] = fb[l];
@@ -431,7 +436,7 @@ __device__ __forceinline__ void cell_adjoint(const AdjArgs& A, int i0, int i1, i
     zouhe_adj<L>(P, miss, aux, kind, fb, auxb);
 #pragma unroll
     for (int l = 0; l < Q; ++l) g[l] = fb[l];
-    if constexpr (PASS == 2) {
+    {
       T* ag = static_cast<T*>(A.aux_grad);
       ag[list_index] = ag[list_index] + auxb;
     }
@@ -448,9 +453,18 @@ __device__ __forceinline__ long long pull_source(const RowOffsets& rows, const i
   return rows.of<L>(l) + z[axis_c<L>(l, 2) + 1];
 }
 
-// Pass 1: every cell, one thread per cell; grid as step_kernel.
+// Pass 1: every cell, one thread per cell; grid as step_kernel.  Fluid cells
+// run the collision adjoint and push; boundary cells zero their push targets.
+// Resident blocks asked of the register allocator for pass 1: the forward
+// kernel's choice for BGK; KBC's adjoint keeps the allocator's choice (its
+// per-cell state does not fit the BGK budget).
+template <class L, class T, bool KBC>
+constexpr int adjoint_min_blocks() {
+  return KBC ? 1 : march_min_blocks<L, T>();
+}
+
 template <class L, int SK, class T, bool KBC>
-__global__ void __launch_bounds__(kStepBlock) adjoint_push_kernel(const AdjArgs A) {
+__global__ void __launch_bounds__(kStepBlock, adjoint_min_blocks<L, T, KBC>()) adjoint_push_kernel(const AdjArgs A) {
   const StepArgs& a = A.s;
   using St = Store<SK, T>;
   using Bits = typename St::Bits;
@@ -467,24 +481,24 @@ __global__ void __launch_bounds__(kStepBlock) adjoint_push_kernel(const AdjArgs 
   const int z[3] = {i2 == n2 - 1 ? 0 : i2 + 1, i2, i2 == 0 ? n2 - 1 : i2 - 1};
   const T* __restrict__ lam_out = static_cast<const T*>(A.lam_out);
   T* __restrict__ lam_in = static_cast<T*>(A.lam_in);
-  const uint8_t id = a.bc_mask[cell];
-  if (id == 255) {
+  if (a.bc_mask[cell] != 0) {
 #pragma unroll
     for (int l = 0; l < Q; ++l) lam_in[(long long)l * N + pull_source<L>(rows, z, l)] = T(0);
     return;
   }
-  T P[Q], g[Q];
+  T P[Q], g[Q], fb[Q];
 #pragma unroll
   for (int l = 0; l < Q; ++l) {
     P[l] = St::dec(ldg_bits(at0<Bits>(a, l, pull_source<L>(rows, z, l))), T(weight<L>(l)));
     g[l] = lam_out[(long long)l * N + cell];
   }
-  cell_adjoint<L, SK, T, KBC, 1>(A, i0, i1, i2, cell, id, P, g, 0);
+  collide_adj<L, T, KBC>(P, omega_of<T>(a), g, fb);
 #pragma unroll
-  for (int l = 0; l < Q; ++l) lam_in[(long long)l * N + pull_source<L>(rows, z, l)] = g[l];
+  for (int l = 0; l < Q; ++l) lam_in[(long long)l * N + pull_source<L>(rows, z, l)] = fb[l];
 }
 
-// Pass 2: the listed boundary cells, one thread per cell.
+// Pass 2: every boundary cell (id != 0), one thread per cell; all writes are
+// atomic additions.
 template <class L, int SK, class T, bool KBC>
 __global__ void __launch_bounds__(kStepBlock) adjoint_bc_kernel(const AdjArgs A) {
   const StepArgs& a = A.s;
@@ -506,13 +520,16 @@ __global__ void __launch_bounds__(kStepBlock) adjoint_bc_kernel(const AdjArgs A)
   const RowOffsets rows(i0, i1, a.n0, n1, n2);
   const int z[3] = {i2 == n2 - 1 ? 0 : i2 + 1, i2, i2 == 0 ? n2 - 1 : i2 - 1};
   const T* __restrict__ lam_out = static_cast<const T*>(A.lam_out);
+  T* __restrict__ lam_in = static_cast<T*>(A.lam_in);
   T P[Q], g[Q];
 #pragma unroll
   for (int l = 0; l < Q; ++l) {
     P[l] = St::dec(ldg_bits(at0<Bits>(a, l, pull_source<L>(rows, z, l))), T(weight<L>(l)));
     g[l] = lam_out[(long long)l * N + cell];
   }
-  cell_adjoint<L, SK, T, KBC, 2>(A, i0, i1, i2, cell, id, P, g, i);
+  cell_adjoint<L, SK, T, KBC>(A, i0, i1, i2, cell, id, P, g, i);
+#pragma unroll
+  for (int l = 0; l < Q; ++l) atomicAdd(lam_in + (long long)l * N + pull_source<L>(rows, z, l), g[l]);
 }
 
 // Launch of both passes for one lattice; returns 0, -1 (unsupported pair) or the CUDA error.

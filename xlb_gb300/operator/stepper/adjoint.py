@@ -30,8 +30,6 @@ import torch
 
 from xlb_gb300 import _lib
 
-_OWN_OR_AUX = (_lib.BC_HALFWAY_BB, _lib.BC_EXTRAPOLATION, _lib.BC_ZOUHE_VELOCITY, _lib.BC_ZOUHE_PRESSURE,
-               _lib.BC_REGULARIZED_VELOCITY, _lib.BC_REGULARIZED_PRESSURE)
 _AUX = (_lib.BC_ZOUHE_VELOCITY, _lib.BC_ZOUHE_PRESSURE, _lib.BC_REGULARIZED_VELOCITY, _lib.BC_REGULARIZED_PRESSURE)
 
 
@@ -63,7 +61,8 @@ class DifferentiableRun:
         self.bits = stepper._aux_state(bc_mask, missing_mask)[0]
         bcs = stepper.boundary_conditions
         kind = {bc.id: bc.kind for bc in bcs}
-        self.bc_cells = _cells_of(bc_mask, [i for i, k in kind.items() if k in _OWN_OR_AUX])
+        # every boundary cell: the adjoint kernel runs their local adjoint in its second pass
+        self.bc_cells = _cells_of(bc_mask, list(kind))
         self.aux_cells = _cells_of(bc_mask, [i for i, k in kind.items() if k in _AUX])
         # position of every aux cell inside bc_cells (both sorted)
         self.aux_pos = torch.searchsorted(self.bc_cells, self.aux_cells)
