@@ -109,7 +109,8 @@ class ClockSampler:
 
 
 def cavity_setup(n, policy_name, omega=1.8):
-    """The cavity: stepper and prepared fields on the current device."""
+    """The cavity: stepper and prepared fields on the current device; n is the
+    cube edge or an (nx, ny, nz) shape."""
     import numpy as np
 
     import xlb_gb300 as xlb
@@ -118,7 +119,7 @@ def cavity_setup(n, policy_name, omega=1.8):
 
     pp = getattr(xlb.PrecisionPolicy, policy_name)
     xlb.init(xlb.velocity_set.D3Q19(pp), xlb.ComputeBackend.CUDA, pp)
-    grid = xlb.grid.grid_factory((n, n, n))
+    grid = xlb.grid.grid_factory((n, n, n) if isinstance(n, int) else tuple(n))
     box = grid.bounding_box_indices()
     nob = grid.bounding_box_indices(remove_edges=True)
     walls = [box["bottom"][i] + box["left"][i] + box["right"][i] + box["front"][i] + box["back"][i] for i in range(3)]

@@ -45,7 +45,7 @@ enum {
   XLBG_STORE_F32 = 0,
   XLBG_STORE_F64 = 1,
   XLBG_STORE_F16 = 2,   /* raw FP16, XLB's FP32FP16 / FP64FP16 */
-  XLBG_STORE_F16S = 3,  /* FP16 holding f - w_l */
+  XLBG_STORE_F16S = 3,  /* FP16 holding (f - w_l) * 2^14 */
   XLBG_STORE_BF16S = 4  /* BF16 holding f - w_l */
 };
 enum { XLBG_COMPUTE_F32 = 0, XLBG_COMPUTE_F64 = 1 };

@@ -104,9 +104,19 @@ def _bf16_to_f32(bits):
     return (bits.astype(np.uint32) << 16).view(np.float32)
 
 
+# The FP16 shifted form stores (f - w_l) * 2^14: the scale keeps deviations
+# down to about 4e-9 in FP16's normal range (its smallest normal is 6.1e-5), where
+# the unscaled form would fall into subnormals with 6e-8 absolute resolution.
+# A power of two scales exactly, so the only roundings are f - w_l in FP32 and
+# the conversion to FP16.
+F16S_SCALE = np.float32(2.0**14)
+F16S_INV_SCALE = np.float32(2.0**-14)
+
+
 class Store:
     """How populations live in memory: 'f64', 'f32', 'f16' (raw) or the shifted
-    'f16s' / 'bf16s' forms (stored value = f - w_l)."""
+    'f16s' / 'bf16s' forms (stored value = (f - w_l) * 2^14 in FP16, f - w_l in
+    BF16)."""
 
     def __init__(self, kind, lattice):
         self.kind = kind
@@ -127,14 +137,14 @@ class Store:
             return f.astype(self.np_dtype)
         dev = (f - self._w(T, f.ndim)).astype(np.float32)
         if self.kind == "f16s":
-            return dev.astype(np.float16)
+            return (dev * F16S_SCALE).astype(np.float16)
         return _bf16_round(dev)
 
     def decode(self, s, T):
         """stored array (q, ...) -> compute-dtype populations."""
         if self.kind in ("f64", "f32", "f16"):
             return s.astype(T)
-        raw = s.astype(np.float32) if self.kind == "f16s" else _bf16_to_f32(s)
+        raw = s.astype(np.float32) * F16S_INV_SCALE if self.kind == "f16s" else _bf16_to_f32(s)
         return raw.astype(T) + self._w(T, s.ndim)
 
     def encode_raw(self, x, T):

@@ -168,3 +168,23 @@ def test_bgk_pair_form_matches_oracle(lattice, shape, layout, policy):
     got0, got1 = sc.gpu_steps(3)
     _compare(got0, want0, "f_0")
     _compare(got1, want1, "f_1")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("env", [{"XLBG_WIDE_OFFSETS": "1"}], ids=["wide"])
+def test_kernel_variants_match_oracle(env):
+    """The marching kernel's 64-bit plane offsets (used when Q x cells >= 2^32),
+    which small grids do not select, forced through XLBG_WIDE_OFFSETS in a child
+    process (the switch is read once per process)."""
+    import os
+    import subprocess
+    import sys
+
+    child_env = dict(os.environ, **env)
+    sel = ("(test_step_matches_oracle or test_store_forms_match_oracle) and "
+           "(channel_regularized or channel_zouhe or cavity_fullway)")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-m", "pytest", os.path.abspath(__file__), "-q", "-x", "-m", "gpu", "-k", sel],
+                       env=child_env, capture_output=True, text=True, cwd=root)
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-2000:]
+    assert " passed" in r.stdout

@@ -252,6 +252,17 @@ static void recovery_pass(const xlbg_desc* d, bool save, void* f, const int64_t*
     recovery_by_size<Lattice<2>>(bytes, save, f, cells, miss, scratch, nrec, n, s);
 }
 
+// XLBG_WIDE_OFFSETS=1 selects the 64-bit plane offsets of the marching kernel at
+// any size (they are needed only when Q * cells >= 2^32); lets small grids check
+// that instantiation against the oracle.
+static bool wide_forced() {
+  static const bool forced = [] {
+    const char* e = getenv("XLBG_WIDE_OFFSETS");
+    return e != nullptr && atoi(e) != 0;
+  }();
+  return forced;
+}
+
 int fill_step_args(const xlbg_desc* d, const void* f0, void* f1, const uint8_t* bc_mask,
                           const uint32_t* miss, double omega, StepArgs& a) {
   a.f0 = f0;
@@ -260,6 +271,7 @@ int fill_step_args(const xlbg_desc* d, const void* f0, void* f1, const uint8_t* 
   a.bc_mask = bc_mask;
   a.miss = miss;
   a.ncell = ncells(d);
+  a.wide = wide_forced() || (long long)lattice_q(d->lattice) * a.ncell > 0xffffffffLL;
   internal_dims(d, a.n0, a.n1, a.n2);
   a.nbc = d->nbc;
   a.omega = omega;
@@ -307,9 +319,8 @@ int launch_main(const xlbg_desc* d, const StepArgs& a, bool diag, cudaStream_t s
   const bool full = needs_full_bc(d) || diag;
   const bool pair = d->collision == XLBG_BGK_PAIR;
   int r = -1;
-  // the marching kernel indexes with 32-bit offsets: every plane offset l * cells + cell must fit
-  const long long q = d->lattice == 0 ? 9 : (d->lattice == 1 ? 19 : 27);
-  if (!diag && q * a.ncell <= 0xffffffffLL) {
+  // the marching kernel keeps cell offsets in 32 bits (plane offsets are 64-bit when a.wide)
+  if (!diag && a.ncell < 0x7fffffffLL) {
     const int threads = a.n2 >= kStepBlock ? kStepBlock : ((a.n2 + 31) / 32) * 32;
     const int chunk = choose_chunk(a, threads);
     if (chunk > 0) {

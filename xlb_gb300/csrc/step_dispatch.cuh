@@ -41,19 +41,29 @@ int launch_step_t(const StepArgs& a, int sk, int compute, bool fullbc, bool diag
   return (int)cudaGetLastError();
 }
 
+// One marching-kernel instantiation family: offset width from a.wide, BC code from fullbc.
+template <class L, int SKV, class TV, int COLL>
+void launch_march_variant(const StepArgs& a, bool fullbc, dim3 grid, int threads, int chunk, cudaStream_t s) {
+  if (a.wide) {
+    if (fullbc)
+      step_kernel_march<L, SKV, TV, COLL, true, long long><<<grid, threads, 0, s>>>(a, chunk);
+    else
+      step_kernel_march<L, SKV, TV, COLL, false, long long><<<grid, threads, 0, s>>>(a, chunk);
+  } else {
+    if (fullbc)
+      step_kernel_march<L, SKV, TV, COLL, true, unsigned><<<grid, threads, 0, s>>>(a, chunk);
+    else
+      step_kernel_march<L, SKV, TV, COLL, false, unsigned><<<grid, threads, 0, s>>>(a, chunk);
+  }
+}
+
 // Marching kernel; `threads` per block (multiple of 32), `chunk` rows of axis 1 per thread.
 template <int LAT, int COLL>
 int launch_step_march_t(const StepArgs& a, int sk, int compute, bool fullbc, int threads, int chunk, cudaStream_t s) {
   using L = Lattice<LAT>;
   const int zblocks = (a.n2 + threads - 1) / threads;
   const dim3 grid((unsigned)(a.n0 * zblocks), (unsigned)((a.n1 + chunk - 1) / chunk));
-#define XLBG_MLAUNCH(SKV, TV)                                                                  \
-  do {                                                                                       \
-    if (fullbc)                                                                              \
-      step_kernel_march<L, SKV, TV, COLL, true><<<grid, threads, 0, s>>>(a, chunk);         \
-    else                                                                                     \
-      step_kernel_march<L, SKV, TV, COLL, false><<<grid, threads, 0, s>>>(a, chunk);        \
-  } while (0)
+#define XLBG_MLAUNCH(SKV, TV) launch_march_variant<L, SKV, TV, COLL>(a, fullbc, grid, threads, chunk, s)
   if (compute == 1) {
     switch (sk) {
       case SK_F64: XLBG_MLAUNCH(SK_F64, double); break;

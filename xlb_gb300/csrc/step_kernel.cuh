@@ -47,6 +47,7 @@ struct StepArgs {
   // or a separate field for the recording and adjoint entry points
   const void* aux;
   long long ncell;
+  int wide;  // Q * ncell >= 2^32: the marching kernel indexes planes in 64 bits
   int n0, n1, n2;
   int nbc;
   double omega;
@@ -353,13 +354,14 @@ constexpr int march_min_blocks() {
   return sizeof(T) != 4 ? 1 : (L::Q <= 19 ? 4 : 2);
 }
 
-template <class L, int SK, class T, int COLL, bool FULLBC>
+// Idx: type of the plane-and-cell offsets, unsigned when Q * cells < 2^32, else
+// long long (cell offsets stay 32-bit: the host runs this kernel for < 2^31 cells).
+template <class L, int SK, class T, int COLL, bool FULLBC, class Idx>
 __global__ void __launch_bounds__(kStepBlock, march_min_blocks<L, T>()) step_kernel_march(const StepArgs a, int chunk) {
   using St = Store<SK, T>;
   using Bits = typename St::Bits;
   constexpr int Q = L::Q;
 
-  // Q * cells < 2^32 here (the host checks), so every offset is 32-bit
   const int n0 = a.n0, n1 = a.n1, n2 = a.n2;
   const int zblocks = (n2 + blockDim.x - 1) / blockDim.x;
   const int i0 = blockIdx.x / zblocks;
@@ -388,9 +390,9 @@ __global__ void __launch_bounds__(kStepBlock, march_min_blocks<L, T>()) step_ker
 #pragma unroll
     for (int l = 0; l < Q; ++l) {
       const unsigned src = xz[axis_c<L>(l, 0) + 1][axis_c<L>(l, 2) + 1] + yo[axis_c<L>(l, 1) + 1];
-      f[l] = St::dec(ldg_bits(at0<Bits>(a, l, src)), T(weight<L>(l)));
+      f[l] = St::dec(ldg_bits(at0<Bits>(a, l, (Idx)src)), T(weight<L>(l)));
     }
-    cell_update<L, SK, T, COLL, FULLBC, false>(a, i0, i1, i2, cell, id, f, dm, df);
+    cell_update<L, SK, T, COLL, FULLBC, false>(a, i0, i1, i2, (Idx)cell, id, f, dm, df);
   }
 }
 

@@ -3,12 +3,13 @@
 Mirrors xlb/precision_policy.py:8-89 (``Precision`` and ``PrecisionPolicy`` with
 the same member names).  Two store forms are new here:
 
-* ``FP32FP16S`` -- populations stored as FP16 *shifted deviations* f_l - w_l,
-  computed in FP32 (the DDF-shifting of Lehmann et al., Phys. Rev. E 106,
-  015308 (2022)).  XLB's ``FP32FP16`` stores raw FP16 and is kept as-is.
-* ``FP32BF16S`` -- the same with BF16 storage.
+* ``FP32FP16S`` -- populations stored as FP16 *shifted deviations*
+  (f_l - w_l) * 2^14, computed in FP32 (the DDF-shifting of Lehmann et al., Phys.
+  Rev. E 106, 015308 (2022); the power-of-two scale keeps small deviations out of
+  FP16's subnormal range).  XLB's ``FP32FP16`` stores raw FP16 and is kept as-is.
+* ``FP32BF16S`` -- f_l - w_l in BF16 (no scale: BF16 has FP32's exponent range).
 
-With shifted storage every population slot holds ``f - w_l`` in the store type,
+With shifted storage every population slot holds the (scaled) ``f - w_l``,
 except the boundary auxiliary value that ZouHe / Regularized keep in slot 0 of
 the aux buffer: that one is stored raw (unshifted), because it is a prescribed
 velocity or density, not a population.
