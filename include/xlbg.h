@@ -214,6 +214,14 @@ int xlbg_adjoint_segment(const xlbg_desc* desc, const void* states, int32_t n_st
                          void* lam_a, void* lam_b, void* aux_grad, double omega, void* stream);
 
 /*
+ * Number of thread blocks of the TMA-staged step (16-bit stores) that gave up
+ * on a bounded wait since the last reset (0 in normal operation); such a block
+ * stores nothing.  Synchronises with the device.  reset != 0 clears the count.
+ * Returns the count, or -XLBG_ERR_CUDA.  No XLB counterpart.
+ */
+int xlbg_device_faults(int reset);
+
+/*
  * f = feq(rho, u) in the store form for every cell (initializers.py:5-20 with
  * quadratic_equilibrium.py:63-82).  rho: (1, cells) and u: (d, cells) in the
  * compute type, or NULL for the uniform values rho0 / u0[d].

@@ -41,6 +41,7 @@ EXPORTED = (
     "xlbg_step_diag_noalloc",
     "xlbg_forward_segment",
     "xlbg_adjoint_segment",
+    "xlbg_device_faults",
     "xlbg_equilibrium",
     "xlbg_macroscopic",
 )
@@ -93,6 +94,7 @@ _SIGNATURES = {
     "xlbg_step_diag_noalloc": ([_DESC, _P, _P, _P, _P, _P, _I64, _D, _I32, _I32, _P, _P], ctypes.c_int),
     "xlbg_forward_segment": ([_DESC, _P, _I32, _P, _P, _P, _D, _P], ctypes.c_int),
     "xlbg_adjoint_segment": ([_DESC, _P, _I32, _P, _P, _P, _P, _I64, _P, _P, _P, _D, _P], ctypes.c_int),
+    "xlbg_device_faults": ([_I32], ctypes.c_int),
     "xlbg_equilibrium": ([_DESC, _P, _P, _D, ctypes.POINTER(_D), _P, _P], ctypes.c_int),
     "xlbg_macroscopic": ([_DESC, _P, _P, _P, _P], ctypes.c_int),
 }

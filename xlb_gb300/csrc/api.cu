@@ -315,8 +315,13 @@ static int choose_chunk(const StepArgs& a, int threads) {
   return (int)chunk;
 }
 
+int try_launch_tma(const xlbg_desc* d, const StepArgs& a, bool fullbc, bool diag, cudaStream_t s);
+
 int launch_main(const xlbg_desc* d, const StepArgs& a, bool diag, cudaStream_t s) {
   const bool full = needs_full_bc(d) || diag;
+  // 16-bit stores: TMA-staged rows when the shape allows (1 = not applicable)
+  const int t = try_launch_tma(d, a, full, diag, s);
+  if (t != 1) return t;
   const bool pair = d->collision == XLBG_BGK_PAIR;
   int r = -1;
   // the marching kernel keeps cell offsets in 32 bits (plane offsets are 64-bit when a.wide)

@@ -1,0 +1,125 @@
+// Host side of the TMA-staged step (step_tma.cuh): applicability, tensor-map
+// encoding, the device error flag of the bounded waits.
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdlib.h>
+
+#include <mutex>
+
+#include "../../include/xlbg.h"
+#include "step_tma.cuh"
+
+namespace xlbg {
+
+int fail(int code, const char* fmt, ...);
+
+// Set by a TMA-staged block whose stage did not complete within its bounded wait.
+__device__ int g_tma_fault = 0;
+
+namespace {
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static const EncodeTiledFn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<EncodeTiledFn>(p);
+  }();
+  return fn;
+}
+
+bool tma_enabled() {
+  static const bool on = [] {
+    const char* e = getenv("XLBG_TMA");
+    return e == nullptr || atoi(e) != 0;
+  }();
+  return on;
+}
+
+std::mutex g_mu;
+int* g_fault_ptr[64] = {nullptr};
+
+int* fault_ptr() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> lock(g_mu);
+  if (!g_fault_ptr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_tma_fault) != cudaSuccess) return nullptr;
+    g_fault_ptr[dev] = static_cast<int*>(p);
+  }
+  return g_fault_ptr[dev];
+}
+
+}  // namespace
+
+// Launches the TMA-staged step when it applies: a 16-bit store with FP32
+// compute (raw FP16 with BGK, FP16/BF16 shifted with pair-form BGK), no
+// diagnostics, a contiguous axis of 8..992 cells that is a multiple of 8, all
+// offsets within 32 bits and a 16-byte aligned f0.  Returns 1 when it does not
+// apply (the caller uses the marching kernel), else the status.
+int try_launch_tma(const xlbg_desc* d, const StepArgs& a, bool fullbc, bool diag, cudaStream_t s) {
+  if (diag || !tma_enabled() || d->compute != XLBG_COMPUTE_F32) return 1;
+  const int sk = d->store;
+  const int coll = d->collision;
+  const bool combo = (sk == SK_F16 && coll == XLBG_BGK) || ((sk == SK_F16S || sk == SK_BF16S) && coll == XLBG_BGK_PAIR);
+  if (!combo) return 1;
+  const int q = d->lattice == XLBG_D2Q9 ? 9 : (d->lattice == XLBG_D3Q19 ? 19 : 27);
+  if (a.n2 < 8 || a.n2 > 992 || a.n2 % 8 != 0) return 1;
+  if ((long long)q * a.ncell > 0xffffffffLL) return 1;
+  if (reinterpret_cast<uintptr_t>(a.f0) % 16 != 0) return 1;
+  EncodeTiledFn enc = encode_fn();
+  int* err = fault_ptr();
+  if (!enc || !err) return 1;
+
+  const int box = a.n2 < kTmaBox ? a.n2 : kTmaBox;
+  CUtensorMap map;
+  const cuuint64_t dims[4] = {(cuuint64_t)a.n2, (cuuint64_t)a.n1, (cuuint64_t)a.n0, (cuuint64_t)q};
+  const cuuint64_t strides[3] = {(cuuint64_t)a.n2 * 2, (cuuint64_t)a.n1 * a.n2 * 2, (cuuint64_t)a.ncell * 2};
+  const cuuint32_t boxdim[4] = {(cuuint32_t)box, 1, 1, 1};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  if (enc(&map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 4, const_cast<void*>(a.f0), dims, strides, boxdim, estr,
+          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return 1;
+
+  // rows of axis 1 per CTA: about eight resident waves of CTAs over 152 SMs
+  const int cps = a.n2 <= 256 ? 4 : (a.n2 <= 512 ? 2 : 1);
+  const long long target = 152LL * cps * 8;
+  long long rows = ((long long)a.n0 * a.n1 + target - 1) / target;
+  if (rows < 1) rows = 1;
+  if (rows > a.n1) rows = a.n1;
+
+  int r;
+  if (d->lattice == XLBG_D2Q9)
+    r = launch_step_tma_d2q9(map, a, sk, coll, fullbc, (int)rows, box, err, s);
+  else if (d->lattice == XLBG_D3Q19)
+    r = launch_step_tma_d3q19(map, a, sk, coll, fullbc, (int)rows, box, err, s);
+  else
+    r = launch_step_tma_d3q27(map, a, sk, coll, fullbc, (int)rows, box, err, s);
+  if (r < 0) return 1;
+  if (r) return fail(XLBG_ERR_CUDA, "TMA step kernel launch: %s", cudaGetErrorString((cudaError_t)r));
+  return XLBG_OK;
+}
+
+}  // namespace xlbg
+
+extern "C" int xlbg_device_faults(int reset) {
+  using namespace xlbg;
+  int* p = fault_ptr();
+  if (!p) return -XLBG_ERR_CUDA;
+  int v = 0;
+  if (cudaMemcpy(&v, p, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return -XLBG_ERR_CUDA;
+  if (reset && v) {
+    const int zero = 0;
+    if (cudaMemcpy(p, &zero, sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) return -XLBG_ERR_CUDA;
+  }
+  return v;
+}
