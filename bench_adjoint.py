@@ -115,6 +115,33 @@ def _c_matrix(stepper, dtype, device):
     return torch.as_tensor(c, dtype=dtype, device=device)
 
 
+def measure_fp32(dim=2, steps=None):
+    """The FP32 forward + backward only (target from an FP32 run), for profiling."""
+    steps = steps or (2000 if dim == 2 else 500)
+    dev = torch.device("cuda")
+    ctx = _build(dim, "FP32FP32", steps)
+    ny = ctx["ny"]
+    y = torch.arange(ny, dtype=torch.float32, device=dev)
+    c32 = _c_matrix(ctx["stepper"], torch.float32, dev)
+    with torch.no_grad():
+        u_target = _velocity(ctx["run"](ctx["f_0"], _aux(ctx, 1.0 + 0.1 * torch.sin(2 * math.pi * y / ny))), c32)
+    loss = _loss_fn(ctx, c32, u_target)
+    times = []
+    for _ in range(2):  # warm-up, timed
+        amp = torch.ones(ny, dtype=torch.float32, device=dev, requires_grad=True)
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        torch.cuda.synchronize()
+        e0.record()
+        L = loss(ctx["f_0"].clone().requires_grad_(True), amp)
+        e1.record()
+        L.backward()
+        e2.record()
+        torch.cuda.synchronize()
+        times.append((e0.elapsed_time(e1), e1.elapsed_time(e2)))
+    return {"steps": steps, "fwd_ms": times[-1][0], "bwd_ms": times[-1][1],
+            "adjoint_to_forward": times[-1][1] / times[-1][0]}
+
+
 def measure(dim=2, steps=None, h=1e-5, fd=True):
     """One differentiation run; returns a dict of the reported figures."""
     steps = steps or (2000 if dim == 2 else 500)
@@ -213,8 +240,9 @@ def main():
     p = argparse.ArgumentParser()
     p.add_argument("--dim", type=int, default=2, choices=[2, 3])
     p.add_argument("--steps", type=int, default=None)
+    p.add_argument("--fp32-only", action="store_true", help="FP32 forward + backward only (no FP64 checks)")
     a = p.parse_args()
-    print(json.dumps(measure(a.dim, a.steps)))
+    print(json.dumps(measure_fp32(a.dim, a.steps) if a.fp32_only else measure(a.dim, a.steps)))
 
 
 if __name__ == "__main__":
