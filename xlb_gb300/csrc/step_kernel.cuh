@@ -157,14 +157,18 @@ __device__ __forceinline__ void store_cell(const StepArgs& a, Idx cell, const T 
   using St = Store<SK, T>;
   using Bits = typename St::Bits;
   T msum = T(0);
-  // the cell's slot in plane 0 plus launch-uniform plane offsets: the offsets can
-  // live in uniform registers (measured 3 % faster than per-store 32-bit offsets)
+  // 16-bit stores address the cell's slot in plane 0 plus launch-uniform plane
+  // offsets (measured 3 % faster for them); 32/64-bit stores keep one 32-bit
+  // plane-and-cell offset per store (3 % faster for FP32)
   Bits* __restrict__ row1 = static_cast<Bits*>(a.f1) + cell;
   const size_t plane = (size_t)a.ncell;
 #pragma unroll
   for (int l = 0; l < L::Q; ++l) {
     const Bits b = St::enc(fo[l], T(weight<L>(l)));
-    row1[(size_t)l * plane] = b;
+    if constexpr (sizeof(Bits) == 2)
+      row1[(size_t)l * plane] = b;
+    else
+      *at1<Bits>(a, l, cell) = b;
     if constexpr (DIAG) {
       const T v = St::dec(b, T(weight<L>(l)));
       msum = l == 0 ? v : msum + v;
