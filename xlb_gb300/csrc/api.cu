@@ -325,7 +325,7 @@ int launch_main(const xlbg_desc* d, const StepArgs& a, bool diag, cudaStream_t s
   const bool pair = d->collision == XLBG_BGK_PAIR;
   int r = -1;
   // the marching kernel keeps cell offsets in 32 bits (plane offsets are 64-bit when a.wide)
-  if (!diag && a.ncell < 0x7fffffffLL) {
+  if (a.ncell < 0x7fffffffLL) {
     const int threads = a.n2 >= kStepBlock ? kStepBlock : ((a.n2 + 31) / 32) * 32;
     const int chunk = choose_chunk(a, threads);
     if (chunk > 0) {

@@ -44,7 +44,12 @@ int launch_step_t(const StepArgs& a, int sk, int compute, bool fullbc, bool diag
 // One marching-kernel instantiation family: offset width from a.wide, BC code from fullbc.
 template <class L, int SKV, class TV, int COLL>
 void launch_march_variant(const StepArgs& a, bool fullbc, dim3 grid, int threads, int chunk, cudaStream_t s) {
-  if (a.wide) {
+  if (a.diag_slots != nullptr) {  // the diagnostics step (always with the full BC code)
+    if (a.wide)
+      step_kernel_march<L, SKV, TV, COLL, true, long long, true><<<grid, threads, 0, s>>>(a, chunk);
+    else
+      step_kernel_march<L, SKV, TV, COLL, true, unsigned, true><<<grid, threads, 0, s>>>(a, chunk);
+  } else if (a.wide) {
     if (fullbc)
       step_kernel_march<L, SKV, TV, COLL, true, long long><<<grid, threads, 0, s>>>(a, chunk);
     else

@@ -364,7 +364,11 @@ constexpr int march_min_blocks() {
 
 // Idx: type of the plane-and-cell offsets, unsigned when Q * cells < 2^32, else
 // long long (cell offsets stay 32-bit: the host runs this kernel for < 2^31 cells).
-template <class L, int SK, class T, int COLL, bool FULLBC, class Idx>
+// DIAG: the diagnostics step (mass of the output, force on the input; see
+// cell_update) -- per-thread FP64 sums over the rows it walks, then the block
+// reduction into the slot array.  Threads past the contiguous axis then stay to
+// the end for the reduction's barrier.
+template <class L, int SK, class T, int COLL, bool FULLBC, class Idx, bool DIAG = false>
 __global__ void __launch_bounds__(kStepBlock, march_min_blocks<L, T>()) step_kernel_march(const StepArgs a, int chunk) {
   using St = Store<SK, T>;
   using Bits = typename St::Bits;
@@ -374,7 +378,10 @@ __global__ void __launch_bounds__(kStepBlock, march_min_blocks<L, T>()) step_ker
   const int zblocks = (n2 + blockDim.x - 1) / blockDim.x;
   const int i0 = blockIdx.x / zblocks;
   const int i2 = (blockIdx.x - i0 * zblocks) * blockDim.x + threadIdx.x;
-  if (i2 >= n2) return;
+  if constexpr (!DIAG) {
+    if (i2 >= n2) return;
+  }
+  const bool inside = i2 < n2;
   const unsigned plane = (unsigned)n1 * (unsigned)n2;
   // source index parts along axes 0 and 2 for c = -1, 0, +1 (index c + 1)
   const unsigned xo[3] = {(unsigned)(i0 == n0 - 1 ? 0 : i0 + 1) * plane, (unsigned)i0 * plane,
@@ -386,7 +393,7 @@ __global__ void __launch_bounds__(kStepBlock, march_min_blocks<L, T>()) step_ker
 #pragma unroll
     for (int q = 0; q < 3; ++q) xz[p][q] = xo[p] + zo[q];
   const int r0 = blockIdx.y * chunk;
-  const int r1 = r0 + chunk < n1 ? r0 + chunk : n1;
+  const int r1 = !inside ? r0 : (r0 + chunk < n1 ? r0 + chunk : n1);
   double dm = 0.0, df[3] = {0.0, 0.0, 0.0};
   for (int i1 = r0; i1 < r1; ++i1) {
     const unsigned yo[3] = {(unsigned)(i1 == n1 - 1 ? 0 : i1 + 1) * (unsigned)n2, (unsigned)i1 * (unsigned)n2,
@@ -400,8 +407,18 @@ __global__ void __launch_bounds__(kStepBlock, march_min_blocks<L, T>()) step_ker
       const unsigned src = xz[axis_c<L>(l, 0) + 1][axis_c<L>(l, 2) + 1] + yo[axis_c<L>(l, 1) + 1];
       f[l] = St::dec(ldg_bits(at0<Bits>(a, l, (Idx)src)), T(weight<L>(l)));
     }
-    cell_update<L, SK, T, COLL, FULLBC, false>(a, i0, i1, i2, (Idx)cell, id, f, dm, df);
+    if constexpr (DIAG) {
+      double dmc = 0.0, dfc[3] = {0.0, 0.0, 0.0};
+      cell_update<L, SK, T, COLL, FULLBC, true>(a, i0, i1, i2, (Idx)cell, id, f, dmc, dfc);
+      dm += dmc;
+      df[0] += dfc[0];
+      df[1] += dfc[1];
+      df[2] += dfc[2];
+    } else {
+      cell_update<L, SK, T, COLL, FULLBC, false>(a, i0, i1, i2, (Idx)cell, id, f, dm, df);
+    }
   }
+  if constexpr (DIAG) reduce_diag(dm, df, a.diag_slots);
 }
 
 }  // namespace xlbg
