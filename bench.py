@@ -188,7 +188,8 @@ def max_over_ranks(x):
         return x
     import torch
 
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if _dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     _dist.all_reduce(t, op=_dist.ReduceOp.MAX)
     return float(t.item())
 
