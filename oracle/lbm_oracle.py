@@ -324,10 +324,40 @@ def bgk(f, feq, omega_t):
     return f - omega_t * (f - feq)
 
 
+def fma32(a, b, c):
+    """Correctly rounded float32 a * b + c (what the CUDA __fmaf_rn and C fmaf give).
+
+    The float64 product of two float32 values is exact; the float64 sum p + c
+    rounds once, and TwoSum recovers its error e exactly.  Rounding the float64
+    sum to float32 is then correct except when it lands exactly on the midpoint
+    between two float32 neighbours while e != 0: the exact value then lies on
+    the side given by the sign of e."""
+    a64 = np.asarray(a, dtype=np.float32).astype(np.float64)
+    b64 = np.asarray(b, dtype=np.float32).astype(np.float64)
+    c64 = np.asarray(c, dtype=np.float32).astype(np.float64)
+    p = a64 * b64
+    s = p + c64
+    bb = s - p
+    e = (p - (s - bb)) + (c64 - bb)
+    r = s.astype(np.float32)
+    r64 = r.astype(np.float64)
+    # the float32 neighbour of r on the side of s, and the midpoint between them
+    toward = np.where(s > r64, np.float32(np.inf), np.float32(-np.inf)).astype(np.float32)
+    n = np.nextafter(r, toward)
+    mid = (r64 + n.astype(np.float64)) * 0.5
+    tie = (s == mid) & (s != r64) & (e != 0)
+    # at a tie, RN picked r or n by parity; the exact value is beyond the midpoint on e's side
+    up = np.where(r64 > n.astype(np.float64), r, n)
+    down = np.where(r64 > n.astype(np.float64), n, r)
+    fixed = np.where(e > 0, up, down)
+    return np.where(tie, fixed, r).astype(np.float32)
+
+
 def bgk_pair(lat, f, omega_t, T):
     """BGK with macroscopic and equilibrium arranged over opposite-direction pairs
     (collision code 2; no XLB counterpart).  Same equations as macroscopic +
-    equilibrium + bgk; the operation order below is the CUDA path's."""
+    equilibrium + bgk; the operation order below is the CUDA path's, including
+    its fused multiply-adds under FP32 compute (fma32)."""
     pairs = [l for l in range(1, lat.q) if l < lat.opp[l]]
     rho = f[0].copy()
     j = [np.zeros_like(rho) for _ in range(lat.d)]
@@ -343,15 +373,16 @@ def bgk_pair(lat, f, omega_t, T):
                 j[d] = j[d] - dif
     inv = T(1.0) / rho
     u = [jd * inv for jd in j]
+    fused = T == np.float32  # FP32 compute fuses multiply-adds, FP64 keeps two roundings
     usq = u[0] * u[0]
     for d in range(1, lat.d):
-        usq = usq + u[d] * u[d]
-    base = T(1.0) - T(1.5) * usq
+        usq = fma32(u[d], u[d], usq) if fused else usq + u[d] * u[d]
+    base = fma32(T(-1.5), usq, T(1.0)) if fused else T(1.0) - T(1.5) * usq
     omf = T(1.0) - omega_t
     orho = omega_t * rho
     w = lat.w.astype(T)
     fo = np.empty_like(f)
-    fo[0] = omf * f[0] + orho * w[0] * base
+    fo[0] = fma32(omf, f[0], orho * w[0] * base) if fused else omf * f[0] + orho * w[0] * base
     for l in pairs:
         o = lat.opp[l]
         cu = np.zeros_like(rho)
@@ -360,11 +391,16 @@ def bgk_pair(lat, f, omega_t, T):
                 cu = cu + u[d]
             elif lat.c[d, l] == -1:
                 cu = cu - u[d]
-        e = base + T(4.5) * (cu * cu)
         t = T(3.0) * cu
         ow = orho * w[l]
-        fo[l] = omf * f[l] + ow * (e + t)
-        fo[o] = omf * f[o] + ow * (e - t)
+        if fused:
+            e = fma32(T(4.5) * cu, cu, base)
+            fo[l] = fma32(omf, f[l], ow * (e + t))
+            fo[o] = fma32(omf, f[o], ow * (e - t))
+        else:
+            e = base + T(4.5) * (cu * cu)
+            fo[l] = omf * f[l] + ow * (e + t)
+            fo[o] = omf * f[o] + ow * (e - t)
     return fo
 
 

@@ -97,10 +97,14 @@ static void FN(bgk_pair)(const lattice_t* L, const T* f, T omega, T* fo) {
   }
   const T inv = (T)1 / rho;
   for (int d = 0; d < L->d; ++d) u[d] = j[d] * inv;
+  /* FP32 compute fuses multiply-adds (fmaf, correctly rounded), as the CUDA path does */
+  const int fused = sizeof(T) == 4;
   T usq = u[0] * u[0];
-  for (int d = 1; d < L->d; ++d) usq = usq + u[d] * u[d];
-  const T base = (T)1 - (T)1.5 * usq, omf = (T)1 - omega, orho = omega * rho;
-  fo[0] = omf * f[0] + orho * (T)L->w[0] * base;
+  for (int d = 1; d < L->d; ++d) usq = fused ? (T)fmaf((float)u[d], (float)u[d], (float)usq) : usq + u[d] * u[d];
+  const T base = fused ? (T)fmaf(-1.5f, (float)usq, 1.0f) : (T)1 - (T)1.5 * usq;
+  const T omf = (T)1 - omega, orho = omega * rho;
+  const T r0 = orho * (T)L->w[0] * base;
+  fo[0] = fused ? (T)fmaf((float)omf, (float)f[0], (float)r0) : omf * f[0] + r0;
   for (int l = 1; l < L->q; ++l) {
     const int o = L->opp[l];
     if (l >= o) continue;
@@ -109,9 +113,18 @@ static void FN(bgk_pair)(const lattice_t* L, const T* f, T omega, T* fo) {
       if (L->c[l][d] == 1) cu = cu + u[d];
       if (L->c[l][d] == -1) cu = cu - u[d];
     }
-    const T e = base + (T)4.5 * (cu * cu), t = (T)3 * cu, ow = orho * (T)L->w[l];
-    fo[l] = omf * f[l] + ow * (e + t);
-    fo[o] = omf * f[o] + ow * (e - t);
+    const T t = (T)3 * cu, ow = orho * (T)L->w[l];
+    if (fused) {
+      const T h = (T)4.5 * cu;
+      const T e = (T)fmaf((float)h, (float)cu, (float)base);
+      const T pl = ow * (e + t), po = ow * (e - t);
+      fo[l] = (T)fmaf((float)omf, (float)f[l], (float)pl);
+      fo[o] = (T)fmaf((float)omf, (float)f[o], (float)po);
+    } else {
+      const T e = base + (T)4.5 * (cu * cu);
+      fo[l] = omf * f[l] + ow * (e + t);
+      fo[o] = omf * f[o] + ow * (e - t);
+    }
   }
 }
 

@@ -259,3 +259,29 @@ def test_bgk_pair_form_equals_bgk_to_rounding(lat):
     want = O.bgk(f, O.equilibrium(L, rho, u, np.float64), 1.7)
     got = O.bgk_pair(L, f, 1.7, np.float64)
     assert np.max(np.abs(got - want)) < 1e-15
+
+
+def test_fma32_is_correctly_rounded():
+    """The oracle's float32 fused multiply-add (used by the pair-form BGK under FP32
+    compute) against exact rational arithmetic, including the double-rounding case
+    where the float64 sum lands exactly on a float32 midpoint."""
+    from fractions import Fraction
+
+    def exact(a, b, c):
+        v = Fraction(float(a)) * Fraction(float(b)) + Fraction(float(c))
+        lo = np.float32(float(v))
+        cands = [np.nextafter(lo, np.float32(-np.inf)), lo, np.nextafter(lo, np.float32(np.inf))]
+        return min(cands, key=lambda x: (abs(Fraction(float(x)) - v), int(np.float32(x).view(np.uint32)) & 1))
+
+    # float64 rounds a*b + c up onto the midpoint of 1+2^-23 and 1+2^-22; the exact value is below it
+    a = np.float32(2.0**-12 * (1 + 2.0**-23))
+    b = np.float32(2.0**-12 * (1 - 2.0**-23))
+    c = np.float32(1 + 2.0**-23)
+    assert O.fma32(a, b, c) == np.float32(1 + 2.0**-23)
+    assert np.float32(np.float64(a) * np.float64(b) + np.float64(c)) != np.float32(1 + 2.0**-23)
+    rng = np.random.default_rng(3)
+    x, y, z = (rng.standard_normal(500).astype(np.float32) for _ in range(3))
+    got = O.fma32(x, y, z)
+    assert all(got[i] == exact(x[i], y[i], z[i]) for i in range(500))
+    got = O.fma32(x, y, (-(x * y)).astype(np.float32))
+    assert all(got[i] == exact(x[i], y[i], -(x[i] * y[i])) for i in range(500))
