@@ -148,8 +148,10 @@ def timed_device(stepper, fields, omega, steps, warmup):
 
 def timed_e2e(stepper, fields, omega, steps):
     """The job through the public API with host buffers: H2D of the initial
-    populations and masks from pinned host memory, K per-step ``stepper(...)``
-    calls with the caller-side swap, D2H of the final populations."""
+    populations and masks from pinned host memory, f_1 made on the device as a
+    copy of f_0 (as prepare_fields makes it, nse_stepper.py:58-98), K per-step
+    ``stepper(...)`` calls with the caller-side swap, D2H of the final
+    populations."""
     import torch
 
     f_0, f_1, bcm, mm = fields
@@ -161,7 +163,7 @@ def timed_e2e(stepper, fields, omega, steps):
     barrier()
     t0 = time.perf_counter()
     f_0.copy_(hf, non_blocking=True)
-    f_1.copy_(hf, non_blocking=True)
+    f_1.copy_(f_0)
     bcm.copy_(hb, non_blocking=True)
     mm.copy_(hm, non_blocking=True)
     for i in range(steps):
@@ -170,7 +172,7 @@ def timed_e2e(stepper, fields, omega, steps):
     hf.copy_(f_0, non_blocking=True)
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
-    h2d = 2 * hf.numel() * hf.element_size() + hb.numel() + hm.numel()
+    h2d = hf.numel() * hf.element_size() + hb.numel() + hm.numel()
     d2h = hf.numel() * hf.element_size()
     return dt, h2d, d2h
 
@@ -346,7 +348,7 @@ def main():
             "unit": "MLUPS",
             "h2d_bytes_per_step": h2d / args.steps,
             "d2h_bytes_per_step": d2h / args.steps,
-            "what": "public stepper(...) call per step with caller swap; initial populations+masks H2D from pinned host and final populations D2H inside the timed region",
+            "what": "public stepper(...) call per step with caller swap; initial populations and masks H2D from pinned host (f_1 = device copy of f_0, as prepare_fields makes it) and final populations D2H inside the timed region",
         }
     if not args.no_adjoint and rank == 0:
         # differentiation: D3Q19 128^3 channel, T=500, checkpoints every 100
