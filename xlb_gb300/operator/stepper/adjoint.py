@@ -15,8 +15,15 @@ Here the same schedule runs on the C ABI:
   segment is still in the buffer after the forward pass and is not replayed.
 
 Memory: ceil(K / k) checkpoints plus k + 1 recorded states plus two adjoint
-fields, k = checkpoint_every.  Compute: one forward pass, one replay (of all
-segments but the last) and one adjoint sweep.
+fields, k = checkpoint_every; the recorded segment, the aux field and the
+adjoint fields belong to the plan and are reused by every call.  Compute: one
+forward pass, one replay (of all segments but the last) and one adjoint sweep.
+
+Each segment's recording and reverse sweep is captured once as a CUDA graph
+(the kernels of k steps in one launch) and replayed afterwards, which matters
+for small grids where a step's kernels take a few microseconds.  A backward
+whose recorded last segment was overwritten by a later forward replays that
+segment from its checkpoint, so interleaved calls stay exact.
 
 The state of the map is the population field; the ZouHe / Regularized
 prescribed values are a separate differentiable input (one value per such
@@ -44,7 +51,7 @@ class DifferentiableRun:
     """``num_steps`` steps of ``stepper`` as a differentiable function
     ``(f_init, aux_values) -> f_final``; call it like a function."""
 
-    def __init__(self, stepper, bc_mask, missing_mask, omega, num_steps, checkpoint_every=100):
+    def __init__(self, stepper, bc_mask, missing_mask, omega, num_steps, checkpoint_every=100, use_graphs=True):
         pp = stepper.precision_policy
         if (pp.store_code, pp.compute_code) not in ((0, 0), (0, 1), (1, 1)):
             raise NotImplementedError(f"the adjoint supports FP32FP32, FP64FP32 and FP64FP64, not {pp}")
@@ -71,6 +78,10 @@ class DifferentiableRun:
         self.state_shape = (stepper.velocity_set.q,) + tuple(stepper.grid.field_shape)
         self.n_cells = stepper.grid.num_cells
         self.peak_buffer_bytes = 0
+        self.use_graphs = use_graphs
+        self._graphs = {}
+        self._states = None
+        self._generation = 0
 
     def aux_from_fields(self, f_1):
         """The prescribed values as prepare_fields stored them (slot 0 of f_1)."""
@@ -107,25 +118,67 @@ class DifferentiableRun:
         nseg = math.ceil(self.num_steps / self.k)
         return [(s * self.k, min(self.k, self.num_steps - s * self.k)) for s in range(nseg)]
 
+    # ------------------------------------------------------------ persistent buffers and graphs
+    def _buffers(self, device):
+        """The recorded segment, the aux field and the adjoint pair, owned by the plan
+        so that captured graphs can replay on them."""
+        if self._states is None:
+            self._states = torch.empty((self.k + 1,) + self.state_shape, dtype=self.store_dtype, device=device)
+            self._aux_buf = torch.zeros(self.n_cells, dtype=self.store_dtype, device=device)
+            self._lam = [torch.empty(self.state_shape, dtype=self.compute_dtype, device=device) for _ in range(2)]
+            self._aux_grad = torch.zeros(max(1, self.bc_cells.numel()), dtype=self.compute_dtype, device=device)
+        return self._states
+
+    def _run_graph(self, key, fn):
+        """fn() once as a captured CUDA graph, replayed on later calls with the same
+        key; direct calls if capture is unavailable."""
+        if self.use_graphs:
+            g = self._graphs.get(key)
+            if g is None:
+                try:
+                    g = torch.cuda.CUDAGraph()
+                    with torch.cuda.graph(g):
+                        fn()
+                    self._graphs[key] = g
+                except Exception:  # capture refused: run the same kernels directly from now on
+                    self.use_graphs = False
+                    self._graphs.clear()
+                    torch.cuda.synchronize()
+                    fn()
+                    return
+            g.replay()
+            return
+        fn()
+
+    def _record(self, n):
+        if n > 0:
+            self._run_graph(("fwd", n), lambda: self._forward(self._states, n, self._aux_buf))
+
+    def _reverse(self, n, swapped):
+        lam_a, lam_b = (self._lam[1], self._lam[0]) if swapped else (self._lam[0], self._lam[1])
+        self._run_graph(("adj", n, swapped),
+                        lambda: self._adjoint(self._states, n, self._aux_buf, lam_a, lam_b, self._aux_grad))
+
 
 class _Run(torch.autograd.Function):
     @staticmethod
     def forward(ctx, f_init, aux_values, plan):
         if tuple(f_init.shape) != plan.state_shape or f_init.dtype != plan.store_dtype or not f_init.is_cuda:
             raise ValueError(f"f_init must be a CUDA {plan.store_dtype} tensor of shape {plan.state_shape}")
+        states = plan._buffers(f_init.device)
         aux_field = plan._aux_field(aux_values)
-        states = torch.empty((plan.k + 1,) + plan.state_shape, dtype=plan.store_dtype, device=f_init.device)
+        plan._aux_buf.copy_(aux_field)
         checkpoints = []
         cur = f_init.detach()
-        n = 0
         for _, n in plan.segments():
             checkpoints.append(cur.clone())
             states[0].copy_(cur)
-            plan._forward(states, n, aux_field)
+            plan._record(n)
             cur = states[n]
         out = cur.clone()
+        plan._generation += 1
+        ctx.generation = plan._generation
         ctx.plan = plan
-        ctx.states = states
         ctx.checkpoints = checkpoints
         ctx.aux_field = aux_field
         ctx.f_dtype = f_init.dtype
@@ -136,20 +189,24 @@ class _Run(torch.autograd.Function):
     @staticmethod
     def backward(ctx, grad_out):
         plan = ctx.plan
-        states = ctx.states
-        lam_a = grad_out.detach().to(plan.compute_dtype).contiguous().clone()
-        lam_b = torch.empty_like(lam_a)
-        aux_grad = torch.zeros(max(1, plan.bc_cells.numel()), dtype=plan.compute_dtype, device=lam_a.device)
+        states = plan._states
+        plan._aux_buf.copy_(ctx.aux_field)
+        plan._lam[0].copy_(grad_out.detach())
+        plan._aux_grad.zero_()
+        # the recorded last segment is this call's only if no later forward overwrote it
+        recorded = ctx.generation == plan._generation
         segs = plan.segments()
+        swapped = False  # True: the current adjoint is in _lam[1]
         for i in range(len(segs) - 1, -1, -1):
             _, n = segs[i]
-            if i != len(segs) - 1:  # the last segment is still recorded in `states`
+            if i != len(segs) - 1 or not recorded:
                 states[0].copy_(ctx.checkpoints[i])
-                plan._forward(states, n - 1, ctx.aux_field)
-            plan._adjoint(states, n, ctx.aux_field, lam_a, lam_b, aux_grad)
+                plan._record(n - 1)
+            plan._reverse(n, swapped)
             if n % 2:
-                lam_a, lam_b = lam_b, lam_a
-        g_aux = aux_grad[plan.aux_pos].to(ctx.aux_dtype) if plan.aux_cells.numel() else None
-        ctx.states = None
+                swapped = not swapped
+        lam = plan._lam[1] if swapped else plan._lam[0]
+        g_aux = plan._aux_grad[plan.aux_pos].to(ctx.aux_dtype) if plan.aux_cells.numel() else None
+        plan._generation += 1  # the recorded segment now holds replayed states
         ctx.checkpoints = None
-        return lam_a.to(ctx.f_dtype), g_aux, None
+        return lam.to(ctx.f_dtype).clone(), g_aux, None

@@ -224,12 +224,12 @@ class IncompressibleNavierStokesStepper(Stepper):
         )
         return f_0, f_1, out
 
-    def differentiable(self, bc_mask, missing_mask, omega, num_steps, checkpoint_every=100):
+    def differentiable(self, bc_mask, missing_mask, omega, num_steps, checkpoint_every=100, use_graphs=True):
         """``num_steps`` steps as a differentiable map (f_init, aux_values) -> f_final,
         backed by the hand-written adjoint (see ``DifferentiableRun``)."""
         from xlb_gb300.operator.stepper.adjoint import DifferentiableRun
 
-        return DifferentiableRun(self, bc_mask, missing_mask, omega, num_steps, checkpoint_every)
+        return DifferentiableRun(self, bc_mask, missing_mask, omega, num_steps, checkpoint_every, use_graphs)
 
 
 __all__ = ["Stepper", "IncompressibleNavierStokesStepper", "Precision"]
