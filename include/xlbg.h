@@ -117,6 +117,10 @@ int xlbg_pack_missing(const xlbg_desc* desc, const uint8_t* missing_mask, uint32
  * type.  Both may be NULL/0 when the BC list has no such BC.  The recovery
  * writes into f0 happen after every pull of the step, which makes the step
  * deterministic where XLB's kernel races (nse_stepper.py:338-342).
+ *
+ * With a 16-bit store the first call on a device does one-time set-up of the
+ * TMA-staged kernel (shared-memory limits, the fault counter's address, see
+ * xlbg_device_faults); make that first call before any stream capture.
  */
 int xlbg_step(const xlbg_desc* desc, void* f0, void* f1, const uint8_t* bc_mask, const uint32_t* miss_bits,
               const int64_t* rec_cells, int64_t n_rec, void* rec_scratch, double omega, int32_t timestep,
