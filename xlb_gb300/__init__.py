@@ -2,8 +2,8 @@
 
 The import surface mirrors XLB's (xlb/__init__.py): ``init``, ``DefaultConfig``,
 ``ComputeBackend``, ``PrecisionPolicy``, ``Precision``, ``velocity_set``,
-``grid``, ``operator`` (boundary conditions, stepper, macroscopic, equilibrium)
-and ``helper``.  Compute runs in hand-written sm_103a CUDA kernels in
+``grid``, ``operator`` (boundary conditions, stepper, macroscopic, equilibrium),
+``helper`` and ``utils`` (field output).  Compute runs in hand-written sm_103a CUDA kernels in
 ``libxlbg.so``, called through a C ABI (include/xlbg.h).
 """
 
@@ -18,7 +18,8 @@ import xlb_gb300.operator.stepper  # noqa: E402,F401
 import xlb_gb300.operator.macroscopic  # noqa: E402,F401
 import xlb_gb300.operator.equilibrium  # noqa: E402,F401
 import xlb_gb300.helper as helper  # noqa: E402
+import xlb_gb300.utils as utils  # noqa: E402
 
 __version__ = "0.1.0"
 
-__all__ = ["ComputeBackend", "Precision", "PrecisionPolicy", "DefaultConfig", "init", "velocity_set", "grid", "helper"]
+__all__ = ["ComputeBackend", "Precision", "PrecisionPolicy", "DefaultConfig", "init", "velocity_set", "grid", "helper", "utils"]
