@@ -239,6 +239,38 @@ int xlbg_equilibrium(const xlbg_desc* desc, const void* rho, const void* u, doub
  */
 int xlbg_macroscopic(const xlbg_desc* desc, const void* f, void* rho, void* u, void* stream);
 
+/*
+ * Mesh boundary masker for one BC: replaces MeshBoundaryMasker.warp_implementation
+ * (xlb/operator/boundary_masker/mesh_boundary_masker.py:185-236) and its kernel
+ * (:150-183).  3D lattices only.  tri: n_tri triangles of 3 float32 vertices
+ * (x, y, z), in grid units; desc gives lattice and grid shape (its store,
+ * compute and BC fields are not read).  Voxel p of the grid padded by one cell
+ * on every side (p = cell index + 1) is solid when its unit box
+ * [p - 1, p] meets a triangle; then every cell whose voxel is solid gets id 255
+ * and every other cell with a solid neighbour x + c_l (l >= 1) gets bc_id and
+ * missing_mask[opp(l)] = 1.  Other cells and directions are not written, so
+ * earlier maskers' marks stay.
+ *
+ * Work list: the padded grid is cut into bricks of brick^3 voxels, numbered
+ * (bx * nby + by) * nbz + bz with nb* = ceil((n* + 2) / brick).  Pair q
+ * (pair_tri[q], pair_brick[q]) tests triangle pair_tri[q] against the voxels of
+ * brick pair_brick[q] that its bounds meet; the list must hold every (triangle,
+ * brick) pair where the triangle's bounds meet a voxel of the brick (extra
+ * pairs and repeats are harmless, pairs with an index out of range are
+ * skipped).  Scratch: tri_scratch n_tri * XLBG_MESH_TRI_FLOATS floats,
+ * solid_scratch (nx+2)*(ny+2)*(nz+2) bytes.
+ *
+ * flags: XLBG_MESH_EDGE_TESTS also applies the projected-edge tests with the
+ * edge terms that pre_compute (:64-97) writes when its nested subscript stores
+ * take effect; without it those terms are zero, as the stores leave them in a
+ * Warp function, and the tests always pass.
+ */
+#define XLBG_MESH_TRI_FLOATS 38
+#define XLBG_MESH_EDGE_TESTS 1
+int xlbg_mesh_mask(const xlbg_desc* desc, const float* tri, int64_t n_tri, const int32_t* pair_tri,
+                   const int32_t* pair_brick, int64_t n_pairs, int32_t brick, int32_t bc_id, int32_t flags,
+                   float* tri_scratch, uint8_t* solid_scratch, uint8_t* bc_mask, uint8_t* missing_mask, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -10,7 +10,15 @@ that holds the XLB source tree).  Semantics modelled:
 * ``@wp.kernel`` + ``wp.launch`` run the kernel body once per thread index, in
   row-major order, sequentially;
 * ``wp.static``, ``wp.constant`` are identities;
-* builtins used by XLB's stepper path: dot, cw_div, abs, sqrt, atomic_add, tid.
+* builtins used by XLB's stepper path: dot, cw_div, abs, sqrt, atomic_add, tid;
+* for the mesh boundary masker: ``mat33`` values (from 9 scalars row by row, a
+  scalar fill, or 3 vectors as columns), ``transpose``, ``cross``, ``normalize``,
+  ``length``, and ``Mesh`` with ``mesh_query_aabb`` (faces whose bounds meet the
+  query box, closed intervals), ``mesh_eval_position`` (u*p0 + v*p1 +
+  (1-u-v)*p2) and ``mesh_eval_face_normal`` (normalize(cross(p1-p0, p2-p0))).
+  ``m[i]`` of a matrix is a copy of row i, so ``m[i][j] = x`` leaves ``m``
+  unchanged, as in Warp's generated code for a local matrix;
+  ``NESTED_STORES_WRITE = True`` makes it write into ``m`` instead.
 
 Python-scope builtin calls on Python floats (``wp.sqrt(3.0)``) evaluate in
 float32, the way Warp types bare Python floats.  Kernel scalar arguments keep
@@ -30,6 +38,7 @@ int32 = np.int32
 int64 = np.int64
 uint8 = np.uint8
 uint32 = np.uint32
+uint64 = np.uint64
 bool = np.bool_  # noqa: A001  (Warp's name)
 
 _vec_types = {}
@@ -68,6 +77,9 @@ class _Vec:
 
     def __setitem__(self, i, x):
         self.v[int(i)] = self.dtype(x)
+        owner = getattr(self, "_owner", None)
+        if owner is not None:
+            owner[0].a[owner[1], int(i)] = x
 
     def _map(self, fn):
         c = type(self).__new__(type(self))
@@ -130,6 +142,9 @@ vec3 = vec3f
 vec2 = vec2f
 
 
+NESTED_STORES_WRITE = False
+
+
 class _Mat:
     __array_ufunc__ = None
 
@@ -140,7 +155,16 @@ class _Mat:
     def __getitem__(self, idx):
         if isinstance(idx, tuple):
             return self.a[tuple(int(i) for i in idx)]
-        return _vec_type(self.a.shape[1], self.dtype)(self.a[int(idx)])
+        row = _vec_type(self.a.shape[1], self.dtype)(self.a[int(idx)])
+        if NESTED_STORES_WRITE:
+            row._owner = (self, int(idx))  # element stores write through (see _Vec.__setitem__)
+        return row
+
+    def __setitem__(self, idx, x):
+        if isinstance(idx, tuple):
+            self.a[tuple(int(i) for i in idx)] = x
+        else:
+            self.a[int(idx)] = np.asarray(list(x), dtype=self.dtype)
 
 
 def mat(shape, dtype=float32):
@@ -151,6 +175,27 @@ def mat(shape, dtype=float32):
         return m
 
     return make
+
+
+def _mat33_ctor(dtype):
+    def make(*args):
+        if len(args) == 1 and not isinstance(args[0], _Vec):
+            return _Mat(np.full((3, 3), args[0]), dtype)
+        if len(args) == 3 and all(isinstance(a, _Vec) for a in args):
+            return _Mat(np.array([list(a.v) for a in args]).T, dtype)  # vectors are columns
+        if len(args) == 9:
+            return _Mat(np.array(args).reshape(3, 3), dtype)
+        raise ValueError(f"mat33 from {len(args)} arguments")
+
+    return make
+
+
+mat33f = mat33 = _mat33_ctor(float32)
+mat33d = _mat33_ctor(float64)
+
+
+def transpose(m):
+    return _Mat(m.a.T.copy(), m.dtype)
 
 
 # ----------------------------------------------------------------------------- arrays
@@ -181,6 +226,8 @@ class _VecArray:
 
 
 def _as_array(a, dtype=None):
+    if isinstance(dtype, type) and issubclass(dtype, _Vec):
+        dtype = dtype.dtype  # array of vectors: trailing axis of the vector's length
     arr = np.asarray(a) if dtype is None else np.asarray(a).astype(dtype)
     return np.ascontiguousarray(arr).view(_Array)
 
@@ -315,6 +362,56 @@ def min(a, b):  # noqa: A001
 
 def length(v):
     return np.sqrt(dot(v, v))
+
+
+def cross(a, b):
+    return type(a)(a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0])
+
+
+def normalize(a):
+    n = length(a)
+    return a / n if n > 0 else type(a)()
+
+
+_meshes = {}
+
+
+class Mesh:
+    """Triangle mesh: points (N, 3), indices (3T,).  ``id`` keys the registry."""
+
+    def __init__(self, points, indices, **kw):
+        self.points = np.asarray(points, dtype=float32)
+        self.indices = np.asarray(indices).astype(np.int64).reshape(-1, 3)
+        tri = self.points[self.indices]  # (T, 3, 3)
+        self.lowers = tri.min(axis=1)
+        self.uppers = tri.max(axis=1)
+        self.id = uint64(len(_meshes) + 1)
+        _meshes[int(self.id)] = self
+
+
+def mesh_query_aabb(mesh_id, lower, upper):
+    m = _meshes[int(mesh_id)]
+    lo = np.array(lower.v, dtype=float32)
+    hi = np.array(upper.v, dtype=float32)
+    hit = np.all((m.lowers <= hi) & (m.uppers >= lo), axis=1)
+    return iter(int(f) for f in np.nonzero(hit)[0])
+
+
+def _mesh_vertex(m, f, k):
+    return vec3f(m.points[m.indices[f, k]])
+
+
+def mesh_eval_position(mesh_id, face, u, v):
+    m = _meshes[int(mesh_id)]
+    p, q, r = (_mesh_vertex(m, face, k) for k in range(3))
+    u, v = float32(u), float32(v)
+    return p * u + q * v + r * (float32(1) - u - v)
+
+
+def mesh_eval_face_normal(mesh_id, face):
+    m = _meshes[int(mesh_id)]
+    p, q, r = (_mesh_vertex(m, face, k) for k in range(3))
+    return normalize(cross(q - p, r - p))
 
 
 def atomic_add(arr, i, value):

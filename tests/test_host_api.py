@@ -109,9 +109,11 @@ def test_overlap_checks(d3q19_fp32):
     check_bc_overlaps([a], 3)
 
 
-def test_mesh_vertices_rejected(d3q19_fp32):
-    with pytest.raises(NotImplementedError):
-        B.HalfwayBounceBackBC(mesh_vertices=np.zeros((3, 3)))
+def test_mesh_vertices_kept_for_the_mesh_masker(d3q19_fp32):
+    v = np.zeros((3, 3))
+    bc = B.HalfwayBounceBackBC(mesh_vertices=v)
+    assert bc.mesh_vertices is v and bc.indices is None
+    check_bc_overlaps([bc], 3)  # BCs without indices take no part in the overlap check
 
 
 def test_extrapolation_global_normal(d3q19_fp32):

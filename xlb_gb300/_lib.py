@@ -30,6 +30,9 @@ BC_EXTRAPOLATION = 8
 
 BGK, KBC, BGK_PAIR = 0, 1, 2
 
+MESH_TRI_FLOATS = 38
+MESH_EDGE_TESTS = 1
+
 EXPORTED = (
     "xlbg_abi_version",
     "xlbg_last_error",
@@ -44,6 +47,7 @@ EXPORTED = (
     "xlbg_device_faults",
     "xlbg_equilibrium",
     "xlbg_macroscopic",
+    "xlbg_mesh_mask",
 )
 
 
@@ -97,6 +101,7 @@ _SIGNATURES = {
     "xlbg_device_faults": ([_I32], ctypes.c_int),
     "xlbg_equilibrium": ([_DESC, _P, _P, _D, ctypes.POINTER(_D), _P, _P], ctypes.c_int),
     "xlbg_macroscopic": ([_DESC, _P, _P, _P, _P], ctypes.c_int),
+    "xlbg_mesh_mask": ([_DESC, _P, _I64, _P, _P, _I64, _I32, _I32, _I32, _P, _P, _P, _P, _P], ctypes.c_int),
 }
 
 

@@ -54,6 +54,7 @@ def _normalize_indices(indices):
 
 class BoundaryCondition(Operator):
     kind = 0
+    mesh_vertices = None  # what an instance reads after the mesh masker dropped its vertices
 
     def __init__(
         self,
@@ -66,8 +67,6 @@ class BoundaryCondition(Operator):
     ):
         self.id = boundary_condition_registry.register_boundary_condition(self.__class__.__name__ + "_" + str(hash(self)))
         super().__init__(velocity_set or DefaultConfig.velocity_set, precision_policy or DefaultConfig.default_precision_policy, compute_backend)
-        if mesh_vertices is not None:
-            raise NotImplementedError("mesh_vertices (MeshBoundaryMasker) is not supported; pass indices")
         self.indices = indices
         self.mesh_vertices = mesh_vertices
         self.implementation_step = implementation_step

@@ -26,7 +26,7 @@ import torch
 from xlb_gb300 import _lib
 from xlb_gb300.default_config import DefaultConfig
 from xlb_gb300.helper.check_boundary_overlaps import check_bc_overlaps
-from xlb_gb300.operator.boundary_masker import IndicesBoundaryMasker
+from xlb_gb300.operator.boundary_masker import IndicesBoundaryMasker, MeshBoundaryMasker
 from xlb_gb300.operator.operator import Operator
 from xlb_gb300.operator.stepper.desc import make_desc
 from xlb_gb300.precision_policy import Precision
@@ -104,10 +104,15 @@ class IncompressibleNavierStokesStepper(Stepper):
 
     def _process_boundary_conditions(self, boundary_conditions, bc_mask, missing_mask):
         check_bc_overlaps(boundary_conditions, self.velocity_set.d)
+        with_vertices = [bc for bc in boundary_conditions if bc.mesh_vertices is not None]
         with_indices = [bc for bc in boundary_conditions if bc.indices is not None]
         if with_indices:
             masker = IndicesBoundaryMasker(self.velocity_set, self.precision_policy)
             bc_mask, missing_mask = masker(with_indices, bc_mask, missing_mask)
+        if self.velocity_set.d == 3 and with_vertices:
+            mesh_masker = MeshBoundaryMasker(self.velocity_set, self.precision_policy)
+            for bc in with_vertices:
+                bc_mask, missing_mask = mesh_masker(bc, bc_mask, missing_mask)
         return bc_mask, missing_mask
 
     def _initialize_auxiliary_data(self, boundary_conditions, f_0, f_1, bc_mask, missing_mask):
