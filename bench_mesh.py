@@ -102,7 +102,7 @@ def main():
     pair_tri, pair_brick = brick_pairs(t, shape, args.brick)
     n_tri = int(t.shape[0])
     rec = torch.empty(n_tri * _lib.MESH_TRI_FLOATS, dtype=torch.float32, device=dev)
-    solid = torch.empty((nx + 2) * (ny + 2) * (nz + 2), dtype=torch.uint8, device=dev)
+    solid = torch.empty(_lib.mesh_solid_bytes(nx, ny, nz), dtype=torch.uint8, device=dev)
     desc = make_desc(vs, pp, shape)
     lib = _lib.load()
     stream = _lib.stream_handle()

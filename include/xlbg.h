@@ -240,6 +240,22 @@ int xlbg_equilibrium(const xlbg_desc* desc, const void* rho, const void* u, doub
 int xlbg_macroscopic(const xlbg_desc* desc, const void* f, void* rho, void* u, void* stream);
 
 /*
+ * Indices boundary masker for one BC: the per-index work of XLB's Warp
+ * IndicesBoundaryMasker kernel (xlb/operator/boundary_masker/
+ * indices_boundary_masker.py:114-156).  indices: (3, n) int64, row-major (all
+ * x, then all y, then all z; z = 0 on a 2D grid), already shifted by any start
+ * index.  Indices outside the grid are skipped.  Each in-grid index gets bc_id;
+ * direction l is missing where index - c_l leaves the grid; when needs_padding
+ * is non-zero and the index is strictly inside the grid (:29-40), every
+ * in-grid pull direction instead marks the push neighbour index + c_l: id
+ * bc_id, direction l missing.  Replaces the one racy launch over all BCs
+ * (:205-218): call it once per BC in list order and a cell that several BCs
+ * touch keeps the last one's id, whatever the thread order.
+ */
+int xlbg_indices_mask(const xlbg_desc* desc, const int64_t* indices, int64_t n, int32_t bc_id, int32_t needs_padding,
+                      uint8_t* bc_mask, uint8_t* missing_mask, void* stream);
+
+/*
  * Mesh boundary masker for one BC: replaces MeshBoundaryMasker.warp_implementation
  * (xlb/operator/boundary_masker/mesh_boundary_masker.py:185-236) and its kernel
  * (:150-183).  3D lattices only.  tri: n_tri triangles of 3 float32 vertices
@@ -257,15 +273,17 @@ int xlbg_macroscopic(const xlbg_desc* desc, const void* f, void* rho, void* u, v
  * brick pair_brick[q] that its bounds meet; the list must hold every (triangle,
  * brick) pair where the triangle's bounds meet a voxel of the brick (extra
  * pairs and repeats are harmless, pairs with an index out of range are
- * skipped).  Scratch: tri_scratch n_tri * XLBG_MESH_TRI_FLOATS floats,
- * solid_scratch (nx+2)*(ny+2)*(nz+2) bytes.
+ * skipped).  Scratch, both 16-byte aligned: tri_scratch n_tri *
+ * XLBG_MESH_TRI_FLOATS floats, solid_scratch XLBG_MESH_SOLID_BYTES(nx, ny, nz)
+ * bytes.
  *
  * flags: XLBG_MESH_EDGE_TESTS also applies the projected-edge tests with the
  * edge terms that pre_compute (:64-97) writes when its nested subscript stores
  * take effect; without it those terms are zero, as the stores leave them in a
  * Warp function, and the tests always pass.
  */
-#define XLBG_MESH_TRI_FLOATS 38
+#define XLBG_MESH_TRI_FLOATS 39
+#define XLBG_MESH_SOLID_BYTES(nx, ny, nz) (((int64_t)((nx) + 2) * ((ny) + 2) * ((nz) + 2) + 15) / 16 * 16)
 #define XLBG_MESH_EDGE_TESTS 1
 int xlbg_mesh_mask(const xlbg_desc* desc, const float* tri, int64_t n_tri, const int32_t* pair_tri,
                    const int32_t* pair_brick, int64_t n_pairs, int32_t brick, int32_t bc_id, int32_t flags,

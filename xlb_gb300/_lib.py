@@ -30,8 +30,13 @@ BC_EXTRAPOLATION = 8
 
 BGK, KBC, BGK_PAIR = 0, 1, 2
 
-MESH_TRI_FLOATS = 38
+MESH_TRI_FLOATS = 39
 MESH_EDGE_TESTS = 1
+
+
+def mesh_solid_bytes(nx, ny, nz):
+    """XLBG_MESH_SOLID_BYTES: the padded grid's flags, rounded up to 16 bytes."""
+    return ((nx + 2) * (ny + 2) * (nz + 2) + 15) // 16 * 16
 
 EXPORTED = (
     "xlbg_abi_version",
@@ -47,6 +52,7 @@ EXPORTED = (
     "xlbg_device_faults",
     "xlbg_equilibrium",
     "xlbg_macroscopic",
+    "xlbg_indices_mask",
     "xlbg_mesh_mask",
 )
 
@@ -101,6 +107,7 @@ _SIGNATURES = {
     "xlbg_device_faults": ([_I32], ctypes.c_int),
     "xlbg_equilibrium": ([_DESC, _P, _P, _D, ctypes.POINTER(_D), _P, _P], ctypes.c_int),
     "xlbg_macroscopic": ([_DESC, _P, _P, _P, _P], ctypes.c_int),
+    "xlbg_indices_mask": ([_DESC, _P, _I64, _I32, _I32, _P, _P, _P], ctypes.c_int),
     "xlbg_mesh_mask": ([_DESC, _P, _I64, _P, _P, _I64, _I32, _I32, _I32, _P, _P, _P, _P, _P], ctypes.c_int),
 }
 

@@ -124,7 +124,7 @@ class MeshBoundaryMasker(Operator):
         pair_tri, pair_brick = brick_pairs(t, shape, self.brick)
         n_tri = int(t.shape[0])
         rec = torch.empty(max(n_tri, 1) * _lib.MESH_TRI_FLOATS, dtype=torch.float32, device=dev)
-        solid = torch.empty((shape[0] + 2) * (shape[1] + 2) * (shape[2] + 2), dtype=torch.uint8, device=dev)
+        solid = torch.empty(_lib.mesh_solid_bytes(*shape), dtype=torch.uint8, device=dev)
         tri_flat = t.reshape(-1) if n_tri else rec
         desc = make_desc(self.velocity_set, self.precision_policy, shape)
         flags = _lib.MESH_EDGE_TESTS if self.edge_tests else 0
