@@ -192,6 +192,7 @@ def test_tma_staged_step_matches_oracle(lattice, shape, layout, policy):
     sc.randomize(seed=12)
     if layout == "periodic":
         sc.bc_mask[0, 1:3, 0:2, 100:140] = 255  # skip cells inside staged rows
+        sc.bc_mask[0, 0, 1:3, 201:206] = 255  # odd bounds: cell pairs with one skip cell
     want0, want1 = sc.oracle_steps(3)
     got0, got1 = sc.gpu_steps(3)
     _compare(got0, want0, "f_0")
@@ -200,18 +201,24 @@ def test_tma_staged_step_matches_oracle(lattice, shape, layout, policy):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("env", [{"XLBG_WIDE_OFFSETS": "1"}], ids=["wide"])
+@pytest.mark.parametrize("env", [{"XLBG_WIDE_OFFSETS": "1"}, {"XLBG_TMA_X2": "1"}], ids=["wide", "tma_two_cell"])
 def test_kernel_variants_match_oracle(env):
-    """The marching kernel's 64-bit plane offsets (used when Q x cells >= 2^32),
-    which small grids do not select, forced through XLBG_WIDE_OFFSETS in a child
-    process (the switch is read once per process)."""
+    """Kernel variants that the default dispatch does not select, forced in a
+    child process (the switches are read once per process): the marching
+    kernel's 64-bit plane offsets (used when Q x cells >= 2^32), and the
+    two-cell packed-arithmetic consumer of the TMA-staged step for pair-form
+    BGK with shifted 16-bit stores (the default there is one cell per
+    consumer)."""
     import os
     import subprocess
     import sys
 
     child_env = dict(os.environ, **env)
-    sel = ("(test_step_matches_oracle or test_store_forms_match_oracle) and "
-           "(channel_regularized or channel_zouhe or cavity_fullway)")
+    if "XLBG_TMA_X2" in env:
+        sel = "test_tma_staged_step_matches_oracle and (f16s or bf16s)"
+    else:
+        sel = ("(test_step_matches_oracle or test_store_forms_match_oracle) and "
+               "(channel_regularized or channel_zouhe or cavity_fullway)")
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     r = subprocess.run([sys.executable, "-m", "pytest", os.path.abspath(__file__), "-q", "-x", "-m", "gpu", "-k", sel],
                        env=child_env, capture_output=True, text=True, cwd=root)

@@ -120,6 +120,47 @@ __host__ __device__ constexpr unsigned tma_smem_bytes() {
   return (unsigned)tma_stages<L>() * L::Q * PITCH * 2 + 16u * tma_stages<L>();
 }
 
+// Producer warp of a TMA-staged step CTA: lane l < Q issues the copies of
+// direction l, row after row, into the S-stage ring at base (see the hand-off
+// described at step_kernel_tma).  A bounded wait that runs out counts one
+// fault, lets the copies still in flight land and returns.
+template <class L, int PITCH>
+__device__ __forceinline__ void tma_produce(const CUtensorMap& map, unsigned base, unsigned full, unsigned empty, int l,
+                                            int i0, int r0, int nr, int n0, int n1, int n2, int box, int* err) {
+  constexpr int Q = L::Q;
+  constexpr int S = tma_stages<L>();
+  constexpr unsigned ROW = PITCH * 2;
+  constexpr unsigned STAGE = Q * ROW;
+  const bool issuer = l < Q;
+  const int nbox = (n2 + box - 1) / box;
+  const unsigned tx_bytes = (unsigned)(Q * nbox * box * 2);
+  const int c0 = issuer ? axis_c<L>(l, 0) : 0, c1 = issuer ? axis_c<L>(l, 1) : 0;
+  const int xs = c0 == 1 ? (i0 == 0 ? n0 - 1 : i0 - 1) : (c0 == -1 ? (i0 == n0 - 1 ? 0 : i0 + 1) : i0);
+  for (int k = 0; k < nr; ++k) {
+    const unsigned s = (unsigned)(k % S);
+    const int u = k / S;
+    const bool ok = u == 0 || mbar_wait(empty + 8 * s, (unsigned)((u - 1) & 1), kTmaWaitNs);
+    if (__any_sync(0xffffffffu, !ok)) {
+      // consumers stopped: report, let the copies still in flight land
+      if (l == 0) {
+        atomicAdd(err, 1);
+        for (int j = k - S + 1; j < k; ++j)
+          if (j >= 0) mbar_wait(full + 8 * (j % S), (unsigned)((j / S) & 1), kTmaWaitNs);
+      }
+      return;
+    }
+    const unsigned bar = full + 8 * s;
+    if (l == 0) mbar_expect_tx(bar, tx_bytes);
+    __syncwarp();
+    if (issuer) {
+      const int y = r0 + k;
+      const int ys = c1 == 1 ? (y == 0 ? n1 - 1 : y - 1) : (c1 == -1 ? (y == n1 - 1 ? 0 : y + 1) : y);
+      for (int b = 0; b < nbox; ++b)
+        tma_load_4d(base + s * STAGE + (unsigned)l * ROW + b * box * 2, &map, b * box, ys, xs, l, bar);
+    }
+  }
+}
+
 // map: 4D tensor map of f0 as (n2, n1, n0, Q) 16-bit elements, box (box, 1, 1, 1)
 // with box = min(n2, 256).  Grid: (n0, ceil(n1 / rows)); CT + 32 threads per
 // block, CT = tma_consumers<PITCH>(): CT consumers (thread i2 owns cell i2 of
@@ -169,36 +210,7 @@ __global__ void __launch_bounds__(tma_consumers<PITCH>() + 32, tma_min_blocks<PI
   __syncthreads();
 
   if (tid >= CT) {
-    // ---- producer warp: lane l < Q issues the copies of direction l ----
-    const int l = tid - CT;
-    const bool issuer = l < Q;
-    const int nbox = (n2 + box - 1) / box;
-    const unsigned tx_bytes = (unsigned)(Q * nbox * box * 2);
-    const int c0 = issuer ? axis_c<L>(l, 0) : 0, c1 = issuer ? axis_c<L>(l, 1) : 0;
-    const int xs = c0 == 1 ? (i0 == 0 ? n0 - 1 : i0 - 1) : (c0 == -1 ? (i0 == n0 - 1 ? 0 : i0 + 1) : i0);
-    for (int k = 0; k < nr; ++k) {
-      const unsigned s = (unsigned)(k % S);
-      const int u = k / S;
-      const bool ok = u == 0 || mbar_wait(empty + 8 * s, (unsigned)((u - 1) & 1), kTmaWaitNs);
-      if (__any_sync(0xffffffffu, !ok)) {
-        // consumers stopped: report, let the copies still in flight land
-        if (l == 0) {
-          atomicAdd(err, 1);
-          for (int j = k - S + 1; j < k; ++j)
-            if (j >= 0) mbar_wait(full + 8 * (j % S), (unsigned)((j / S) & 1), kTmaWaitNs);
-        }
-        return;
-      }
-      const unsigned bar = full + 8 * s;
-      if (l == 0) mbar_expect_tx(bar, tx_bytes);
-      __syncwarp();
-      if (issuer) {
-        const int y = r0 + k;
-        const int ys = c1 == 1 ? (y == 0 ? n1 - 1 : y - 1) : (c1 == -1 ? (y == n1 - 1 ? 0 : y + 1) : y);
-        for (int b = 0; b < nbox; ++b)
-          tma_load_4d(base + s * STAGE + (unsigned)l * ROW + b * box * 2, &map, b * box, ys, xs, l, bar);
-      }
-    }
+    tma_produce<L, PITCH>(map, base, full, empty, tid - CT, i0, r0, nr, n0, n1, n2, box, err);
     return;
   }
 
@@ -264,6 +276,8 @@ int launch_tma_t(const CUtensorMap& map, const StepArgs& a, bool fullbc, int row
   if (a.n2 <= 512) return launch_tma_pitch<L, SK, COLL, 512>(map, a, fullbc, rows, box, err, s);
   return launch_tma_pitch<L, SK, COLL, 1024>(map, a, fullbc, rows, box, err, s);
 }
+
+bool tma_x2_enabled();
 
 // Per-lattice entry points (step_tma_*.cu).  sk: SK_F16 (XLB-order BGK) or
 // SK_F16S / SK_BF16S (pair-form BGK); other combinations return -1.

@@ -12,6 +12,19 @@
 
 namespace xlbg {
 
+// XLBG_TMA_X2=1 runs pair-form BGK with shifted 16-bit stores on the two-cell
+// consumer kernel (step_tma_x2.cuh; same results).  Off by default: at 512^3
+// D3Q19 it ran at 55.5 / 56.3 GLUPS (FP16S / BF16S) against the one-cell
+// kernel's 58.3 / 58.4 -- half the consumer warps per SM hide less latency
+// than the packed arithmetic saves.
+bool tma_x2_enabled() {
+  static const bool on = [] {
+    const char* e = getenv("XLBG_TMA_X2");
+    return e != nullptr && atoi(e) != 0;
+  }();
+  return on;
+}
+
 int fail(int code, const char* fmt, ...);
 
 // Set by a TMA-staged block whose stage did not complete within its bounded wait.
