@@ -289,6 +289,40 @@ int xlbg_mesh_mask(const xlbg_desc* desc, const float* tri, int64_t n_tri, const
                    const int32_t* pair_brick, int64_t n_pairs, int32_t brick, int32_t bc_id, int32_t flags,
                    float* tri_scratch, uint8_t* solid_scratch, uint8_t* bc_mask, uint8_t* missing_mask, void* stream);
 
+/*
+ * Mesh renderer: the per-pixel ray cast and shading of the MeshRenderer operator
+ * of XLB's out-of-core example (examples/out_of_core/operators/mesh_renderer.py:
+ * 81-187): camera and ray as there, closest hit with t < depth[i, j], vertex
+ * colours interpolated with the hit's barycentrics, normal-based shading,
+ * gamma; RGBA (pixel: height x width x 4 floats) and depth written on a hit
+ * only.  XLB takes the hit from Warp's mesh BVH query; here it comes from a
+ * walk through a uniform grid of triangle lists (xlbg_tri_grid, built by the
+ * caller: cell (cx, cy, cz) spans lo + cell * (cx, cy, cz) .. + cell and is
+ * numbered (cx * dims[1] + cy) * dims[2] + cz; cell_tris[cell_start[k] ..
+ * cell_start[k + 1]) lists every triangle whose bounds meet cell k, a superset
+ * being fine) with the watertight ray-triangle test (Woop, Benthin and Wald,
+ * JCGT 2013); among equal t the lowest face index wins.  face_out (optional,
+ * height x width int32) receives the hit face or -1.  err_count (one int32)
+ * counts list entries skipped as malformed.  points: n_points x 3 floats;
+ * indices: n_tri x 3 int32; vertex_colors: n_points x 3 floats.
+ */
+typedef struct {
+  float lo[3];
+  float cell[3];
+  int32_t dims[3];
+  const int32_t* cell_start;
+  const int32_t* cell_tris;
+} xlbg_tri_grid;
+
+typedef struct {
+  float eye[3], target[3], up[3];
+  float fov_degrees, ambient_intensity, edge_sharpness, gamma;
+} xlbg_camera;
+
+int xlbg_render_mesh(const float* points, int64_t n_points, const int32_t* indices, int64_t n_tri,
+                     const float* vertex_colors, const xlbg_tri_grid* grid, const xlbg_camera* camera, int32_t height,
+                     int32_t width, float* pixel, float* depth, int32_t* face_out, int32_t* err_count, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -55,6 +55,8 @@ class _Vec:
             vals = [dt(0)] * n
         elif len(args) == 1 and hasattr(args[0], "__len__") and not isinstance(args[0], str):
             vals = [dt(v) for v in args[0]]
+        elif len(args) == 1 and n > 1:  # a scalar fills every component
+            vals = [dt(args[0])] * n
         else:
             vals = [dt(v) for v in args]
         if len(vals) != n:
@@ -194,6 +196,13 @@ mat33f = mat33 = _mat33_ctor(float32)
 mat33d = _mat33_ctor(float64)
 
 
+def mat44(*args):
+    """16 scalars, row by row."""
+    if len(args) != 16:
+        raise ValueError(f"mat44 from {len(args)} arguments")
+    return _Mat(np.array([float32(a) for a in args]).reshape(4, 4), float32)
+
+
 def transpose(m):
     return _Mat(m.a.T.copy(), m.dtype)
 
@@ -278,10 +287,22 @@ def func(f):
     return call
 
 
+class _Kernel:
+    """A kernel object (not a function, so a kernel defined in a class body is
+    not bound to instances, as with Warp's Kernel)."""
+
+    def __init__(self, f):
+        self.f = f
+        self.__name__ = getattr(f, "__name__", "kernel")
+
+    def __call__(self, *args):
+        return self.f(*args)
+
+
 def kernel(f=None, **kw):
     if f is None:
-        return lambda g: g
-    return f
+        return lambda g: _Kernel(g)
+    return _Kernel(f)
 
 
 _current_tid = None
@@ -377,12 +398,14 @@ _meshes = {}
 
 
 class Mesh:
-    """Triangle mesh: points (N, 3), indices (3T,).  ``id`` keys the registry."""
+    """Triangle mesh: points (N, 3), indices (3T,).  ``id`` keys the registry;
+    ``mesh_get(id)`` returns the mesh itself (its ``points`` and flat ``indices``)."""
 
     def __init__(self, points, indices, **kw):
         self.points = np.asarray(points, dtype=float32)
-        self.indices = np.asarray(indices).astype(np.int64).reshape(-1, 3)
-        tri = self.points[self.indices]  # (T, 3, 3)
+        self.indices = np.asarray(indices).astype(np.int64).reshape(-1)
+        self.tri_index = self.indices.reshape(-1, 3)
+        tri = self.points[self.tri_index]  # (T, 3, 3)
         self.lowers = tri.min(axis=1)
         self.uppers = tri.max(axis=1)
         self.id = uint64(len(_meshes) + 1)
@@ -398,7 +421,84 @@ def mesh_query_aabb(mesh_id, lower, upper):
 
 
 def _mesh_vertex(m, f, k):
-    return vec3f(m.points[m.indices[f, k]])
+    return vec3f(m.points[m.tri_index[f, k]])
+
+
+def mesh_get(mesh_id):
+    return _meshes[int(mesh_id)]
+
+
+class _RayQuery:
+    def __init__(self, result, t=0.0, u=0.0, v=0.0, sign=1.0, normal=None, face=-1):
+        self.result = result
+        self.t, self.u, self.v, self.sign, self.face = float32(t), float32(u), float32(v), float32(sign), int32(face)
+        self.normal = normal if normal is not None else vec3f()
+
+
+def _woop(org, d, p, q, r):
+    """Watertight ray-triangle test (Woop, Benthin, Wald, JCGT 2013) in float32,
+    without its double-precision fallback: (hit, t, u, v), u weighting p, v q."""
+    ad = [abs(d[0]), abs(d[1]), abs(d[2])]
+    kz = 0
+    if ad[1] > ad[kz]:
+        kz = 1
+    if ad[2] > ad[kz]:
+        kz = 2
+    kx = (kz + 1) % 3
+    ky = (kx + 1) % 3
+    if d[kz] < 0:
+        kx, ky = ky, kx
+    sx = d[kx] / d[kz]
+    sy = d[ky] / d[kz]
+    sz = float32(1) / d[kz]
+    a, b, c = p - org, q - org, r - org
+    ax = a[kx] - sx * a[kz]
+    ay = a[ky] - sy * a[kz]
+    bx = b[kx] - sx * b[kz]
+    by = b[ky] - sy * b[kz]
+    cx = c[kx] - sx * c[kz]
+    cy = c[ky] - sy * c[kz]
+    U = cx * by - cy * bx
+    V = ax * cy - ay * cx
+    W = bx * ay - by * ax
+    if (U < 0 or V < 0 or W < 0) and (U > 0 or V > 0 or W > 0):
+        return False, 0, 0, 0
+    det = (U + V) + W
+    if det == 0:
+        return False, 0, 0, 0
+    T = (U * (sz * a[kz]) + V * (sz * b[kz])) + W * (sz * c[kz])
+    rcp = float32(1) / det
+    t = T * rcp
+    if not t >= 0:
+        return False, 0, 0, 0
+    return True, t, U * rcp, V * rcp
+
+
+def mesh_query_ray(mesh_id, start, direction, max_t):
+    """Closest hit with t < max_t over all faces; equal t keeps the lower face."""
+    m = _meshes[int(mesh_id)]
+    org = vec3f(start)
+    d = vec3f(direction)
+    best = None
+    min_t = float32(max_t)
+    for f in range(m.tri_index.shape[0]):
+        p, q, r = (_mesh_vertex(m, f, k) for k in range(3))
+        hit, t, u, v = _woop(org, d, p, q, r)
+        if hit and t < min_t:
+            min_t = t
+            best = (t, u, v, f, normalize(cross(q - p, r - p)))
+    if best is None:
+        return _RayQuery(False)
+    t, u, v, f, n = best
+    return _RayQuery(True, t, u, v, 1.0, n, f)
+
+
+def pow(x, y):  # noqa: A001
+    return float32(np.power(float32(x), float32(y)))
+
+
+def clamp(x, lo, hi):
+    return lo if x < lo else (hi if x > hi else x)
 
 
 def mesh_eval_position(mesh_id, face, u, v):

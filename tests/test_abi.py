@@ -23,6 +23,28 @@ def declared_symbols():
     return sorted(names)
 
 
+def test_struct_layouts_match_the_header(tmp_path):
+    """sizeof / offsetof of the C structs (gcc on include/xlbg.h) equal the ctypes mirrors."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "layout.c"
+    src.write_text(
+        "#include <stdio.h>\n#include <stddef.h>\n#include \"xlbg.h\"\n"
+        "int main(void) { printf(\"%zu %zu %zu %zu %zu %zu %zu\\n\", sizeof(xlbg_desc), offsetof(xlbg_desc, bc),"
+        " sizeof(xlbg_bc), sizeof(xlbg_tri_grid), offsetof(xlbg_tri_grid, cell_start), sizeof(xlbg_camera),"
+        " offsetof(xlbg_camera, gamma)); return 0; }\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    want = [ctypes.sizeof(_lib.Desc), _lib.Desc.bc.offset, ctypes.sizeof(_lib.BCEntry), ctypes.sizeof(_lib.TriGrid),
+            _lib.TriGrid.cell_start.offset, ctypes.sizeof(_lib.Camera), _lib.Camera.gamma.offset]
+    assert got == want
+
+
 def test_library_loads_and_exports_every_declared_symbol():
     lib = _lib.load()
     names = declared_symbols()

@@ -17,7 +17,7 @@ import pytest
 from oracle import lbm_oracle as O
 
 GOLDEN = sorted(p for p in glob.glob(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "*.npz"))
-          if not os.path.basename(p).startswith("mesh_"))  # mesh_*.npz: tests/test_mesh_masker.py
+          if not os.path.basename(p).startswith(("mesh_", "render_")))  # those: test_mesh_masker.py, test_renderer.py
 
 
 def load(path):

@@ -54,6 +54,7 @@ EXPORTED = (
     "xlbg_macroscopic",
     "xlbg_indices_mask",
     "xlbg_mesh_mask",
+    "xlbg_render_mesh",
 )
 
 
@@ -84,6 +85,32 @@ class Desc(ctypes.Structure):
     ]
 
 
+class TriGrid(ctypes.Structure):
+    """xlbg_tri_grid: uniform grid of triangle lists for xlbg_render_mesh."""
+
+    _fields_ = [
+        ("lo", ctypes.c_float * 3),
+        ("cell", ctypes.c_float * 3),
+        ("dims", ctypes.c_int32 * 3),
+        ("cell_start", ctypes.c_void_p),
+        ("cell_tris", ctypes.c_void_p),
+    ]
+
+
+class Camera(ctypes.Structure):
+    """xlbg_camera."""
+
+    _fields_ = [
+        ("eye", ctypes.c_float * 3),
+        ("target", ctypes.c_float * 3),
+        ("up", ctypes.c_float * 3),
+        ("fov_degrees", ctypes.c_float),
+        ("ambient_intensity", ctypes.c_float),
+        ("edge_sharpness", ctypes.c_float),
+        ("gamma", ctypes.c_float),
+    ]
+
+
 _lock = threading.Lock()
 _lib = None
 
@@ -108,6 +135,8 @@ _SIGNATURES = {
     "xlbg_equilibrium": ([_DESC, _P, _P, _D, ctypes.POINTER(_D), _P, _P], ctypes.c_int),
     "xlbg_macroscopic": ([_DESC, _P, _P, _P, _P], ctypes.c_int),
     "xlbg_indices_mask": ([_DESC, _P, _I64, _I32, _I32, _P, _P, _P], ctypes.c_int),
+    "xlbg_render_mesh": ([_P, _I64, _P, _I64, _P, ctypes.POINTER(TriGrid), ctypes.POINTER(Camera), _I32, _I32,
+                          _P, _P, _P, _P, _P], ctypes.c_int),
     "xlbg_mesh_mask": ([_DESC, _P, _I64, _P, _P, _I64, _I32, _I32, _I32, _P, _P, _P, _P, _P], ctypes.c_int),
 }
 
