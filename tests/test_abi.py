@@ -110,3 +110,55 @@ def test_xlbg_error_carries_message():
     with pytest.raises(_lib.XlbgError) as e:
         _lib.check(_step(_desc(collision=_lib.KBC)))
     assert e.value.code == _lib.ERR_UNSUPPORTED
+
+
+def test_masker_and_renderer_entries_reject_bad_arguments():
+    """Host-side checks of xlbg_indices_mask, xlbg_mesh_mask and xlbg_render_mesh
+    (each returns before any CUDA call)."""
+    lib = _lib.load()
+    p = ctypes.c_void_p
+    d = _desc()
+    # indices masker: bad id, negative count, misaligned index array, 2D grid with nz != 1
+    assert lib.xlbg_indices_mask(d, p(1024), 4, 0, 0, p(4096), p(8192), None) == _lib.ERR_ARG
+    assert lib.xlbg_indices_mask(d, p(1024), -1, 3, 0, p(4096), p(8192), None) == _lib.ERR_ARG
+    assert lib.xlbg_indices_mask(d, p(1028), 4, 3, 0, p(4096), p(8192), None) == _lib.ERR_ALIGN
+    assert lib.xlbg_indices_mask(_desc(lattice=0, nz=2), p(1024), 4, 3, 0, p(4096), p(8192), None) == _lib.ERR_ARG
+    assert lib.xlbg_indices_mask(d, p(1024), 0, 3, 0, None, None, None) == _lib.OK  # nothing to do
+    # mesh masker: 2D lattice, unknown flag, bad brick, unaligned scratch
+    args = dict(tri=p(1024), n=12, pt=p(2048), pb=p(4096), npairs=12, brick=8, bid=4, flags=0, rec=p(8192),
+                solid=p(16384), bm=p(32768), mm=p(65536))
+
+    def mesh(desc, **kw):
+        a = dict(args, **kw)
+        return lib.xlbg_mesh_mask(desc, a["tri"], a["n"], a["pt"], a["pb"], a["npairs"], a["brick"], a["bid"],
+                                  a["flags"], a["rec"], a["solid"], a["bm"], a["mm"], None)
+
+    assert mesh(_desc(lattice=0, nz=1)) == _lib.ERR_UNSUPPORTED
+    assert mesh(d, flags=4) == _lib.ERR_ARG
+    assert mesh(d, brick=0) == _lib.ERR_ARG
+    assert mesh(d, bid=255) == _lib.ERR_ARG
+    assert mesh(d, solid=p(16385)) == _lib.ERR_ALIGN
+    assert mesh(d, rec=p(8196)) == _lib.ERR_ALIGN
+    assert mesh(d, pt=None) == _lib.ERR_ARG
+    # renderer: missing grid / camera, bad dims, non-positive cells, unaligned buffers
+    g = _lib.TriGrid()
+    g.cell[:] = [1.0, 1.0, 1.0]
+    g.dims[:] = [2, 2, 2]
+    g.cell_start = p(1024)
+    g.cell_tris = p(2048)
+    cam = _lib.Camera()
+
+    def render(grid, camera, pixel=p(4096), depth=p(8192), err=p(16384), h=4, w=4):
+        return lib.xlbg_render_mesh(p(32768), 3, p(65536), 1, p(131072), grid, camera, h, w, pixel, depth, None, err,
+                                    None)
+
+    assert render(None, ctypes.byref(cam)) == _lib.ERR_ARG
+    assert render(ctypes.byref(g), None) == _lib.ERR_ARG
+    assert render(ctypes.byref(g), ctypes.byref(cam), h=0) == _lib.ERR_ARG
+    assert render(ctypes.byref(g), ctypes.byref(cam), pixel=p(4098)) == _lib.ERR_ALIGN
+    assert render(ctypes.byref(g), ctypes.byref(cam), err=None) == _lib.ERR_ARG
+    g.dims[:] = [0, 2, 2]
+    assert render(ctypes.byref(g), ctypes.byref(cam)) == _lib.ERR_ARG
+    g.dims[:] = [2, 2, 2]
+    g.cell[:] = [1.0, 0.0, 1.0]
+    assert render(ctypes.byref(g), ctypes.byref(cam)) == _lib.ERR_ARG
