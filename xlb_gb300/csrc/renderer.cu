@@ -81,9 +81,13 @@ __global__ void render_kernel(const float* __restrict__ pts, long long n_points,
                               const float* __restrict__ colors, const Grid g, const Cam cam, int height, int width,
                               float* __restrict__ pixel, float* __restrict__ depth, int32_t* __restrict__ face_out,
                               int* __restrict__ err) {
-  const long long pix = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (pix >= (long long)height * width) return;
-  const int i = (int)(pix / width), j = (int)(pix % width);
+  // a block covers 16 x 8 pixels, each warp an 8 x 4 tile (neighbouring rays walk
+  // neighbouring cells, so the warp's lanes stay together longer)
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.y * 8 + (warp >> 1) * 4 + (lane >> 3);
+  const int j = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
+  if (i >= height || j >= width) return;
+  const long long pix = (long long)i * width + j;
   // ---- the ray (mesh_renderer.py:98-123) ----
   const float aspect = (float)width / (float)height;
   const float fov = cam.fov_degrees * 0.017453292519943295f;
@@ -222,8 +226,7 @@ extern "C" int xlbg_render_mesh(const float* points, int64_t n_points, const int
                                 int32_t height, int32_t width, float* pixel, float* depth, int32_t* face_out,
                                 int32_t* err_count, void* stream) {
   if (!grid || !camera) return fail(XLBG_ERR_ARG, "grid or camera is NULL");
-  if (n_points < 0 || n_tri < 0 || n_tri >= (1LL << 31) || height < 1 || width < 1 ||
-      (long long)height * width >= (1LL << 40))
+  if (n_points < 0 || n_tri < 0 || n_tri >= (1LL << 31) || height < 1 || width < 1 || height > 65535 * 8)
     return fail(XLBG_ERR_ARG, "bad sizes");
   if (grid->dims[0] < 1 || grid->dims[1] < 1 || grid->dims[2] < 1 ||
       (long long)grid->dims[0] * grid->dims[1] * grid->dims[2] >= (1LL << 31) - 1)
@@ -253,8 +256,8 @@ extern "C" int xlbg_render_mesh(const float* points, int64_t n_points, const int
   c.ambient = camera->ambient_intensity;
   c.sharpness = camera->edge_sharpness;
   c.gamma = camera->gamma;
-  const long long np = (long long)height * width;
-  render_kernel<<<(unsigned)((np + 127) / 128), 128, 0, static_cast<cudaStream_t>(stream)>>>(
+  const dim3 blocks((unsigned)((width + 15) / 16), (unsigned)((height + 7) / 8));
+  render_kernel<<<blocks, 128, 0, static_cast<cudaStream_t>(stream)>>>(
       points, n_points, indices, n_tri, vertex_colors, g, c, height, width, pixel, depth, face_out, err_count);
   const cudaError_t r = cudaGetLastError();
   if (r != cudaSuccess) return fail(XLBG_ERR_CUDA, "render launch: %s", cudaGetErrorString(r));
