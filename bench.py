@@ -151,29 +151,36 @@ def timed_e2e(stepper, fields, omega, steps):
     populations and masks from pinned host memory, f_1 made on the device as a
     copy of f_0 (as prepare_fields makes it, nse_stepper.py:58-98), K per-step
     ``stepper(...)`` calls with the caller-side swap, D2H of the final
-    populations."""
+    populations into a pinned result buffer.
+
+    The result buffer is not the input buffer: on the GB300 machine a 10.2 GB D2H
+    into the pinned pages that the job's H2D had read ran at 16-20 GB/s (523-621
+    ms), into other pinned pages at about 180 GB/s (57 ms).  Both host buffers
+    are allocated and written once before the timed region."""
     import torch
 
     f_0, f_1, bcm, mm = fields
-    hf = torch.empty(f_0.shape, dtype=f_0.dtype, pin_memory=True)
-    hf.copy_(f_0)
+    h_in = torch.empty(f_0.shape, dtype=f_0.dtype, pin_memory=True)
+    h_in.copy_(f_0)
+    h_out = torch.empty(f_0.shape, dtype=f_0.dtype, pin_memory=True)
+    h_out.copy_(f_0)
     hb = bcm.cpu().pin_memory()
     hm = mm.cpu().pin_memory()
     torch.cuda.synchronize()
     barrier()
     t0 = time.perf_counter()
-    f_0.copy_(hf, non_blocking=True)
+    f_0.copy_(h_in, non_blocking=True)
     f_1.copy_(f_0)
     bcm.copy_(hb, non_blocking=True)
     mm.copy_(hm, non_blocking=True)
     for i in range(steps):
         f_0, f_1 = stepper(f_0, f_1, bcm, mm, omega, i)
         f_0, f_1 = f_1, f_0
-    hf.copy_(f_0, non_blocking=True)
+    h_out.copy_(f_0, non_blocking=True)
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
-    h2d = hf.numel() * hf.element_size() + hb.numel() + hm.numel()
-    d2h = hf.numel() * hf.element_size()
+    h2d = h_in.numel() * h_in.element_size() + hb.numel() + hm.numel()
+    d2h = h_out.numel() * h_out.element_size()
     return dt, h2d, d2h
 
 
@@ -348,7 +355,7 @@ def main():
             "unit": "MLUPS",
             "h2d_bytes_per_step": h2d / args.steps,
             "d2h_bytes_per_step": d2h / args.steps,
-            "what": "public stepper(...) call per step with caller swap; initial populations and masks H2D from pinned host (f_1 = device copy of f_0, as prepare_fields makes it) and final populations D2H inside the timed region",
+            "what": "public stepper(...) call per step with caller swap; initial populations and masks H2D from pinned host (f_1 = device copy of f_0, as prepare_fields makes it) and final populations D2H into a separate pinned result buffer, inside the timed region",
         }
     if not args.no_adjoint and rank == 0:
         # differentiation: D3Q19 128^3 channel, T=500, checkpoints every 100
