@@ -145,7 +145,8 @@ def _gpu_apply(lat_name, bc_mask, missing, meshes, edges=False, brick=8):
     bm = torch.from_numpy(bc_mask.copy()).cuda()
     mm = torch.from_numpy(missing.copy()).cuda()
     for verts, bid in meshes:
-        masker.apply(np.asarray(verts, dtype=np.float32).reshape(-1, 3, 3), bid, bm, mm)
+        masker.apply(verts if torch.is_tensor(verts) else np.asarray(verts, dtype=np.float32).reshape(-1, 3, 3), bid,
+                     bm, mm)
     torch.cuda.synchronize()
     return bm.cpu().numpy(), mm.cpu().numpy()
 
@@ -245,3 +246,18 @@ def test_stepper_with_mesh_bc_matches_oracle(lattice):
     torch.cuda.synchronize()
     assert np.array_equal(g0.cpu().numpy(), want[0])
     assert np.array_equal(g1.cpu().numpy(), want[1])
+
+
+@pytest.mark.gpu
+def test_gpu_apply_accepts_torch_triangles():
+    """Triangles as a host tensor or a CUDA tensor give the numpy path's marks."""
+    import torch
+
+    shape = (21, 17, 15)
+    tri = _soup(21, shape, 60)
+    prior_bm = np.zeros((1,) + shape, np.uint8)
+    prior_mm = np.zeros((19,) + shape, bool)
+    want = _gpu_apply("D3Q19", prior_bm, prior_mm, [(tri, 6)])
+    for t in (torch.from_numpy(tri), torch.from_numpy(tri).cuda()):
+        got = _gpu_apply("D3Q19", prior_bm, prior_mm, [(t, 6)])
+        assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1])

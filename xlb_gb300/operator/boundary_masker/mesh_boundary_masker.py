@@ -111,7 +111,9 @@ class MeshBoundaryMasker(Operator):
         return bc_mask, missing_mask
 
     def apply(self, tri, bc_id, bc_mask, missing_mask):
-        """Mark (bc_mask, missing_mask) in place from (T, 3, 3) float32 triangles."""
+        """Mark (bc_mask, missing_mask) in place from (T, 3, 3) triangles (numpy
+        array or torch tensor, converted to float32; a pinned host tensor is
+        copied to the GPU asynchronously)."""
         if bc_mask.dtype != torch.uint8 or missing_mask.dtype not in (torch.bool, torch.uint8):
             raise TypeError("bc_mask must be uint8 and missing_mask bool or uint8")
         if not (bc_mask.is_cuda and missing_mask.is_cuda and bc_mask.is_contiguous() and missing_mask.is_contiguous()):
@@ -120,7 +122,10 @@ class MeshBoundaryMasker(Operator):
         if tuple(missing_mask.shape) != (self.velocity_set.q,) + shape:
             raise ValueError("missing_mask must have shape (q, nx, ny, nz) of bc_mask's grid")
         dev = bc_mask.device
-        t = torch.as_tensor(np.asarray(tri, dtype=np.float32).reshape(-1, 3, 3), device=dev)
+        if torch.is_tensor(tri):
+            t = tri.to(device=dev, dtype=torch.float32, non_blocking=True).reshape(-1, 3, 3).contiguous()
+        else:
+            t = torch.as_tensor(np.asarray(tri, dtype=np.float32).reshape(-1, 3, 3), device=dev)
         pair_tri, pair_brick = brick_pairs(t, shape, self.brick)
         n_tri = int(t.shape[0])
         rec = torch.empty(max(n_tri, 1) * _lib.MESH_TRI_FLOATS, dtype=torch.float32, device=dev)

@@ -146,7 +146,7 @@ class MeshRenderer:
         if face_buffer is not None and (tuple(face_buffer.shape) != (h, w) or face_buffer.dtype != torch.int32
                                         or not face_buffer.is_cuda or not face_buffer.is_contiguous()):
             raise ValueError("face_buffer must be a contiguous int32 CUDA tensor of shape (height, width)")
-        grid, keep = mesh.grid()
+        grid, _ = mesh.grid()  # the list tensors stay alive in the mesh
         cam = _lib.Camera()
         cam.eye[:] = _vec(camera_pos)
         cam.target[:] = _vec(camera_target)
@@ -165,5 +165,4 @@ class MeshRenderer:
                 )
             )
         self.last_errors = err  # skipped malformed list entries (0 for lists built by Mesh)
-        del keep
         return pixel_buffer, depth_buffer
