@@ -153,10 +153,10 @@ def timed_e2e(stepper, fields, omega, steps):
     ``stepper(...)`` calls with the caller-side swap, D2H of the final
     populations into a pinned result buffer.
 
-    The result buffer is not the input buffer: on the GB300 machine a 10.2 GB D2H
-    into the pinned pages that the job's H2D had read ran at 16-20 GB/s (523-621
-    ms), into other pinned pages at about 180 GB/s (57 ms).  Both host buffers
-    are allocated and written once before the timed region."""
+    The result buffer is not the input buffer: on a GB300 with a Grace host a
+    10.2 GB D2H into the pinned pages that the job's H2D had read ran at 16-20
+    GB/s (523-621 ms), into other pinned pages at about 180 GB/s (57 ms).  Both
+    host buffers are allocated and written once before the timed region."""
     import torch
 
     f_0, f_1, bcm, mm = fields
