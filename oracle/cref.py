@@ -10,7 +10,6 @@ import ctypes
 import numpy as np
 
 from oracle import build_oracle
-from oracle import lbm_oracle as O
 
 _lib = None
 KINDS = {
