@@ -169,3 +169,54 @@ def test_gpu_sphere_scene_matches_oracle(cells):
     opix, odep, oface = R.render(pts, ind, colors, opix, depth.copy(), **cam)
     _compare(pix, dep, opix, odep, face, oface)
     assert (face >= 0).mean() > 0.3
+
+
+def test_mesh_and_renderer_reject_bad_inputs():
+    import torch
+
+    from xlb_gb300.operator.renderer import Mesh, MeshRenderer
+
+    pts = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    with pytest.raises(ValueError, match="3 entries"):
+        Mesh(pts, [0, 1], device="cpu")
+    with pytest.raises(ValueError, match="outside the point array"):
+        Mesh(pts, [0, 1, 3], device="cpu")
+    with pytest.raises(ValueError, match="finite"):
+        Mesh(np.where(pts > 0, np.nan, pts), [0, 1, 2], device="cpu")
+    mesh = Mesh(pts, [0, 1, 2], device="cpu")
+    assert mesh.num_triangles == 1
+    r = MeshRenderer()
+    with pytest.raises(TypeError):
+        r((pts, [0, 1, 2]), np.ones((3, 3)), torch.zeros(4, 4, 4), torch.zeros(4, 4))
+    with pytest.raises(ValueError, match="pixel_buffer"):
+        r(mesh, np.ones((3, 3)), torch.zeros(4, 4, 4), torch.zeros(4, 4))  # host tensors
+    with pytest.raises(ValueError, match="pixel_buffer"):
+        r(mesh, np.ones((3, 3)), torch.zeros(4, 4, 3), torch.zeros(4, 4))
+
+
+@pytest.mark.parametrize("case", ["empty", "single", "flat", "line"])
+def test_grid_edge_cases(case):
+    import torch
+
+    from xlb_gb300.operator.renderer.mesh_renderer import build_grid
+
+    if case == "empty":
+        pts, ind = np.zeros((0, 3), np.float32), np.zeros(0, np.int64)
+    elif case == "single":
+        pts, ind = np.array([[0.1, 0.2, 0.3], [1.5, 0.2, 0.3], [0.1, 2.0, 0.7]], np.float32), np.arange(3)
+    elif case == "flat":  # a square of 8 triangles in the plane z = 1
+        g = np.stack(np.meshgrid(np.arange(3.0), np.arange(3.0), indexing="ij"), -1).reshape(-1, 2)
+        pts = np.concatenate([g, np.ones((9, 1))], 1).astype(np.float32)
+        ind = np.array([[i * 3 + j, i * 3 + j + 3, i * 3 + j + 1, i * 3 + j + 1, i * 3 + j + 3, i * 3 + j + 4]
+                        for i in range(2) for j in range(2)]).reshape(-1)
+    else:  # degenerate triangles along a line
+        pts = np.array([[0, 0, 0], [1, 0, 0], [2, 0, 0], [3, 0, 0]], np.float32)
+        ind = np.array([0, 1, 2, 1, 2, 3])
+    g, (start, tris) = build_grid(torch.from_numpy(pts), torch.from_numpy(ind.reshape(-1, 3).astype(np.int64)))
+    dims = list(g.dims)
+    assert all(d >= 1 for d in dims) and all(c > 0 for c in g.cell)
+    assert start.numel() == dims[0] * dims[1] * dims[2] + 1
+    n_tri = len(ind) // 3
+    assert int(start[-1]) == (0 if n_tri == 0 else tris.numel())
+    if n_tri:  # every triangle is listed somewhere
+        assert set(tris.tolist()) == set(range(n_tri))
