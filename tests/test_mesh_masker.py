@@ -100,6 +100,37 @@ def test_brick_pairs_cover_every_candidate():
             assert {(int(t), b) for t in need} <= have, (brick, b)
 
 
+def test_brick_pairs_equal_the_direct_expansion():
+    """Exactly the (triangle, brick) pairs whose bricks hold a voxel the
+    triangle's bounds meet, each once (random soups, several brick sizes)."""
+    import itertools
+
+    import torch
+
+    from xlb_gb300.operator.boundary_masker.mesh_boundary_masker import brick_pairs
+
+    rng = np.random.default_rng(0)
+    for trial in range(12):
+        shape = tuple(int(v) for v in rng.integers(3, 30, 3))
+        n = int(rng.integers(0, 60))
+        hi = np.array(shape) - 1e-3
+        tri = rng.uniform(0, 1, (n, 3, 3)) * hi
+        if n:
+            tri[: n // 2] = tri[: n // 2, :1] + rng.uniform(-0.5, 0.5, (n // 2, 3, 3))  # small ones
+        tri = np.clip(tri, 0, hi).astype(np.float32)
+        pdim = np.array(shape) + 2
+        for brick in (1, 3, 8):
+            pt, pb = brick_pairs(torch.from_numpy(tri), shape, brick)
+            nbd = (pdim + brick - 1) // brick
+            want = []
+            for t in range(n):
+                lo = np.maximum(np.ceil(tri[t].min(0).astype(np.float64)), 0).astype(int)
+                up = np.minimum(np.floor(tri[t].max(0).astype(np.float64)) + 1, pdim - 1).astype(int)
+                for bx, by, bz in itertools.product(*[range(lo[k] // brick, up[k] // brick + 1) for k in range(3)]):
+                    want.append((t, int((bx * nbd[1] + by) * nbd[2] + bz)))
+            assert sorted(zip(pt.tolist(), pb.tolist())) == sorted(want), (trial, brick)
+
+
 def test_operator_checks_follow_xlb():
     import torch
 

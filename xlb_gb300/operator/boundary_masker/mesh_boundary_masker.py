@@ -37,7 +37,8 @@ def brick_pairs(tri, shape, brick):
     the padded grid (p = cell index + 1 per axis) is the box [p - 1, p]; a
     triangle's bounds [lo, hi] meet it iff lo <= p and hi >= p - 1, i.e. p in
     [ceil(lo), floor(hi) + 1].  Returns (pair_tri, pair_brick) int32 tensors on
-    tri's device, bricks numbered (bx * nby + by) * nbz + bz, pairs grouped by
+    tri's device, bricks numbered (bx * nby + by) * nbz + bz: first the
+    triangles that lie in one brick, then the pairs of the others, grouped by
     triangle.
     """
     dev = tri.device
@@ -57,15 +58,25 @@ def brick_pairs(tri, shape, brick):
     total = int(counts.sum())
     if total >= (1 << 38):
         raise ValueError(f"{total} (triangle, brick) pairs; use a larger brick")
-    tid = torch.repeat_interleave(torch.arange(tri.shape[0], device=dev), counts)
-    r = torch.arange(total, device=dev) - (torch.cumsum(counts, 0) - counts)[tid]
-    e = ext[tid]
-    b = blo[tid]
+    # triangles within one brick (most of a fine mesh) give one pair each directly;
+    # the others are expanded brick by brick
+    one = counts == 1
+    tid1 = torch.nonzero(one).view(-1)
+    b1 = blo[tid1]
+    bid1 = (b1[:, 0] * nbd[1] + b1[:, 1]) * nbd[2] + b1[:, 2]
+    many = torch.nonzero(counts > 1).view(-1)
+    cm = counts[many]
+    nm = total - int(tid1.numel())
+    k = torch.repeat_interleave(torch.arange(many.numel(), device=dev), cm)
+    tidm = many[k]
+    r = torch.arange(nm, device=dev) - (torch.cumsum(cm, 0) - cm)[k]
+    e = ext[tidm]
+    b = blo[tidm]
     bz = b[:, 2] + r % e[:, 2]
     by = b[:, 1] + (r // e[:, 2]) % e[:, 1]
     bx = b[:, 0] + r // (e[:, 2] * e[:, 1])
-    bid = (bx * nbd[1] + by) * nbd[2] + bz
-    return tid.to(torch.int32), bid.to(torch.int32)
+    bidm = (bx * nbd[1] + by) * nbd[2] + bz
+    return torch.cat([tid1, tidm]).to(torch.int32), torch.cat([bid1, bidm]).to(torch.int32)
 
 
 def triangles(mesh_vertices):
