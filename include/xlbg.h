@@ -53,8 +53,11 @@ enum { XLBG_COMPUTE_F32 = 0, XLBG_COMPUTE_F64 = 1 };
 /* collision (xlb/operator/collision/bgk.py:30-34, kbc.py:192-296).  XLBG_BGK_PAIR is BGK
    with macroscopic and equilibrium rearranged over opposite-direction pairs (one
    reciprocal for u, shared pair terms): the same equations with fewer operations,
-   results equal to XLBG_BGK up to rounding.  No XLB counterpart. */
-enum { XLBG_BGK = 0, XLBG_KBC = 1, XLBG_BGK_PAIR = 2 };
+   results equal to XLBG_BGK up to rounding.  XLBG_BGK_SHIFTED is the pair form
+   evaluated on the stored deviations g = S (f - w_l) of the shifted stores
+   (XLBG_STORE_F16S / XLBG_STORE_BF16S only): one conversion per pulled and per
+   stored value, no FP32 rounding of f itself.  No XLB counterpart for 2 and 3. */
+enum { XLBG_BGK = 0, XLBG_KBC = 1, XLBG_BGK_PAIR = 2, XLBG_BGK_SHIFTED = 3 };
 
 /* boundary-condition kinds (xlb/operator/boundary_condition/bc_*.py) */
 enum {
@@ -85,7 +88,7 @@ typedef struct {
   int32_t lattice;     /* XLBG_D2Q9 / XLBG_D3Q19 / XLBG_D3Q27 */
   int32_t store;       /* XLBG_STORE_* */
   int32_t compute;     /* XLBG_COMPUTE_* */
-  int32_t collision;   /* XLBG_BGK / XLBG_KBC / XLBG_BGK_PAIR */
+  int32_t collision;   /* XLBG_BGK / XLBG_KBC / XLBG_BGK_PAIR / XLBG_BGK_SHIFTED */
   int32_t nbc;         /* entries used in bc[] */
   int64_t nx, ny, nz;  /* grid shape; nz = 1 for 2D */
   xlbg_bc bc[XLBG_MAX_BC];
@@ -164,7 +167,9 @@ int xlbg_step_diag(const xlbg_desc* desc, void* f0, void* f1, const uint8_t* bc_
  * must not exceed XLBG_NOALLOC_REC_SCRATCH_BYTES (XLBG_ERR_ARG otherwise).
  * The first call on a device looks up the arrays' device addresses
  * (cudaGetSymbolAddress) for the calling thread's current device; make that
- * first call before any stream capture.  The arrays are shared by all calls on
+ * first call before any stream capture.  A call that finds the device's
+ * context changed since (after cudaDeviceReset) looks them up again, as a
+ * first call does.  The arrays are shared by all calls on
  * a device: calls whose GPU work may overlap race on them and must be
  * serialised by the caller.  Same results as xlbg_step_diag.
  */
@@ -172,6 +177,20 @@ int xlbg_step_diag(const xlbg_desc* desc, void* f0, void* f1, const uint8_t* bc_
 int xlbg_step_diag_noalloc(const xlbg_desc* desc, void* f0, void* f1, const uint8_t* bc_mask,
                            const uint32_t* miss_bits, const int64_t* rec_cells, int64_t n_rec, double omega,
                            int32_t timestep, int32_t force_id, double* diag, void* stream);
+
+/*
+ * Momentum-exchange force on one no-slip BC (halfway or fullway bounce-back),
+ * replacing MomentumTransfer(no_slip_bc)(f_0, f_1, bc_mask, missing_mask)
+ * (xlb/operator/force/momentum_transfer.py:92-176).  At every cell with
+ * bc_mask == bc_id whose rest direction is not missing, each missing direction
+ * l adds phi_l = 2 f0[opp l] signed by c[opp l] (the no-slip functionals give
+ * f_post_stream[l] = f0[opp l] there); per-cell sums in the compute type, the
+ * sum over cells in FP64.  missing_mask is XLB's bool (Q, cells) field.
+ * diag_slots: XLBG_DIAG_SLOTS x 4 doubles, zero on entry and left zero; force:
+ * 4 doubles, [0, F_x, F_y, F_z] (F_z = 0 in 2D).  Asynchronous on stream.
+ */
+int xlbg_momentum_transfer(const xlbg_desc* desc, const void* f0, const uint8_t* bc_mask, const uint8_t* missing_mask,
+                           int32_t bc_id, double* diag_slots, double* force, void* stream);
 
 /*
  * Differentiation.  XLB differentiates its stepper by taping Warp kernels
@@ -216,6 +235,29 @@ int xlbg_forward_segment(const xlbg_desc* desc, void* states, int32_t n_steps, c
 int xlbg_adjoint_segment(const xlbg_desc* desc, const void* states, int32_t n_steps, const uint8_t* bc_mask,
                          const uint32_t* miss_bits, const void* aux, const int64_t* bc_cells, int64_t n_bc,
                          void* lam_a, void* lam_b, void* aux_grad, double omega, void* stream);
+
+/*
+ * Test hook: which step kernel the step entry points launch, process-wide.
+ * XLBG_KERNEL_AUTO (the default) picks by store, shape and size; the others
+ * force a variant the automatic choice takes only on grids too large for a
+ * test (64-bit plane offsets, used when Q * cells >= 2^32), or never on a given
+ * shape, so that tests can compare every variant with the CPU restatement on
+ * small grids.  Not thread-safe with concurrent steps; set it between steps.
+ *   XLBG_KERNEL_MARCH       marching kernel (no TMA staging)
+ *   XLBG_KERNEL_MARCH_WIDE  marching kernel with 64-bit plane offsets
+ *   XLBG_KERNEL_CELL        one-cell-per-thread kernel (64-bit offsets)
+ *   XLBG_KERNEL_TMA_WIDE    TMA-staged kernel with 64-bit plane offsets where
+ *                           it applies, else the marching kernel with them
+ * Returns XLBG_OK, or XLBG_ERR_ARG for an unknown selector.  No XLB counterpart.
+ */
+enum {
+  XLBG_KERNEL_AUTO = 0,
+  XLBG_KERNEL_MARCH = 1,
+  XLBG_KERNEL_MARCH_WIDE = 2,
+  XLBG_KERNEL_CELL = 3,
+  XLBG_KERNEL_TMA_WIDE = 4
+};
+int xlbg_debug_force_kernel(int32_t kernel);
 
 /*
  * Number of thread blocks of the TMA-staged step (16-bit stores) that gave up

@@ -159,6 +159,30 @@ class Store:
             return _bf16_to_f32(np.asarray(s)).astype(T)
         return np.asarray(s).astype(T)
 
+    # The shifted forms as the deviation-space collision (code 3) sees them:
+    # g = scale * (f - w_l) is the stored value itself.
+    @property
+    def scale(self):
+        return F16S_SCALE if self.kind == "f16s" else np.float32(1.0)
+
+    def deviation(self, s):
+        """stored array -> float32 g (exact)."""
+        return s.astype(np.float32) if self.kind == "f16s" else _bf16_to_f32(s)
+
+    def encode_deviation(self, g):
+        """float32 g -> stored array (round to nearest even)."""
+        g = np.asarray(g, dtype=np.float32)
+        return g.astype(np.float16) if self.kind == "f16s" else _bf16_round(g)
+
+    def to_deviation(self, f):
+        """float32 f (q, ...) -> g = RN(scale f - scale w_l), one rounding (a fused multiply-add)."""
+        sw = (self.scale * self._w(np.float32, f.ndim)).astype(np.float32)
+        return fma32(f, self.scale, -sw)
+
+    def from_deviation(self, g):
+        """float32 g (q, ...) -> f = RN(g / scale + w_l), one rounding; equals decode()."""
+        return fma32(g, np.float32(1.0) / self.scale, self._w(np.float32, g.ndim))
+
 
 # ----------------------------------------------------------------------------
 # Boundary-condition descriptions
@@ -404,6 +428,67 @@ def bgk_pair(lat, f, omega_t, T):
     return fo
 
 
+def bgk_shifted(lat, g, omega_t, scale):
+    """BGK on the stored deviations g = scale (f - w_l) of the shifted stores
+    (collision code 3; no XLB counterpart).  Same equations as macroscopic +
+    equilibrium + bgk (bgk.py:30-34, quadratic_equilibrium.py:35-60) in pair
+    form, rewritten for g:
+      rho = 1 + G/scale, v = 3u = 3 J/(scale rho), base = 1 - |v|^2/6,
+      per weight class k: A = omega scale w_k, C = A rho base - A,
+      per pair (l, o) with t = c_l.v: R = C + (A rho / 2) t^2,
+      g_out_l = (1 - omega) g_l + (A rho t + R), g_out_o = (1 - omega) g_o + (-A rho t + R).
+    FP32 only; the operation order (and every fused multiply-add, fma32) is the
+    CUDA path's."""
+    f32 = np.float32
+    S = f32(scale)
+    K = f32(1.0) / S
+    pairs = [l for l in range(1, lat.q) if l < lat.opp[l]]
+    G = g[0].copy()
+    J = [np.zeros_like(G) for _ in range(lat.d)]
+    for l in pairs:
+        o = lat.opp[l]
+        sig = g[l] + g[o]
+        dif = g[l] - g[o]
+        G = G + sig
+        for d in range(lat.d):
+            if lat.c[d, l] == 1:
+                J[d] = J[d] + dif
+            elif lat.c[d, l] == -1:
+                J[d] = J[d] - dif
+    rho = fma32(K, G, f32(1.0))
+    inv = f32(1.0) / rho
+    k3 = f32(3.0) * (K * inv)
+    v = [Jd * k3 for Jd in J]
+    vsq = v[0] * v[0]
+    for d in range(1, lat.d):
+        vsq = fma32(v[d], v[d], vsq)
+    base = fma32(f32(-1.0) / f32(6.0), vsq, f32(1.0))
+    omf = f32(1.0) - f32(omega_t)
+    norm1 = np.abs(lat.c).sum(axis=0)
+    Ar, Arh, C = {}, {}, {}
+    for k in sorted(set(norm1.tolist())):
+        wk = lat.w[int(np.argmax(norm1 == k))].astype(np.float32)
+        A = f32(omega_t) * (S * wk)
+        Ar[k] = A * rho
+        Arh[k] = f32(0.5) * Ar[k]
+        C[k] = fma32(Ar[k], base, -A)
+    go = np.empty_like(g)
+    go[0] = fma32(omf, g[0], C[0])
+    for l in pairs:
+        o = lat.opp[l]
+        k = int(norm1[l])
+        t = None
+        for d in range(lat.d):
+            if lat.c[d, l] != 0:
+                x = v[d] if lat.c[d, l] == 1 else -v[d]
+                t = x if t is None else t + x
+        q = Arh[k] * t
+        R = fma32(q, t, C[k])
+        go[l] = fma32(omf, g[l], fma32(Ar[k], t, R))
+        go[o] = fma32(omf, g[o], fma32(-Ar[k], t, R))
+    return go
+
+
 def second_moment(lat, fneq, T):
     nt = lat.d * (lat.d + 1) // 2
     pi = []
@@ -571,6 +656,8 @@ def step(lat, store, f0, f1, bc_mask, missing, omega, bcs, collision="BGK", T=np
     the recovered slots, which is what a launch gives when the ZouHe /
     Regularized cells run before the cells reading them.
     """
+    if collision == "BGK_SHIFTED":
+        return _step_shifted(lat, store, f0, f1, bc_mask, missing, omega, bcs, recovery)
     shp = f0.shape[1:]
     ids = bc_mask[0]
     f0c = store.decode(f0, T)
@@ -643,6 +730,74 @@ def step(lat, store, f0, f1, bc_mask, missing, omega, bcs, collision="BGK", T=np
     if skip.any():
         f1_new[:, skip] = f1[:, skip]
 
+    return _recovered(lat, f0, f1, bc_mask, missing, bcs), f1_new
+
+
+def _step_shifted(lat, store, f0, f1, bc_mask, missing, omega, bcs, recovery):
+    """step() with collision code 3 (shifted stores, FP32): every pulled value,
+    streaming-step result and collision output is a stored deviation g.  The
+    bounce-back kinds copy deviations (w_l = w_opp(l)), the extrapolation blend
+    is the same linear expression on g, and EquilibriumBC / ZouHe / Regularized
+    run on f between one from_deviation and one to_deviation per direction."""
+    if not store.shifted:
+        raise ValueError("BGK_SHIFTED needs a shifted store")
+    T = np.float32
+    shp = f0.shape[1:]
+    ids = bc_mask[0]
+    g0 = store.deviation(f0)
+    g0r = g0 if recovery == "after" else store.deviation(_recovered(lat, f0, f1, bc_mask, missing, bcs, with_slot0=False))
+    gps = pull(lat, g0r)
+    for bc in bcs:
+        if bc.kind not in STREAMING_KINDS:
+            continue
+        m = ids == bc.id
+        if not m.any():
+            continue
+        gp = gps[:, m]
+        miss = missing[:, m]
+        own = g0[:, m]
+        if bc.kind in ("halfway_bb", "extrapolation"):
+            for l in range(lat.q):
+                gp[l] = np.where(miss[l], own[lat.opp[l]], gp[l])
+        elif bc.kind == "equilibrium":
+            rho_bc = np.full(gp.shape[1], T(bc.rho), dtype=T)
+            u_bc = [np.full(gp.shape[1], T(bc.u[d]), dtype=T) for d in range(lat.d)]
+            gp = store.to_deviation(equilibrium(lat, rho_bc, u_bc, T))
+        else:
+            aux = store.decode_raw(f1[0][m], T)
+            gp = store.to_deviation(zouhe_like(lat, store.from_deviation(gp), miss, aux, bc.kind, T))
+        gps[:, m] = gp
+
+    gout = bgk_shifted(lat, gps, T(omega), store.scale)
+
+    for bc in bcs:
+        m = ids == bc.id
+        if not m.any():
+            continue
+        if bc.kind == "fullway_bb":
+            gout[:, m] = gps[:, m][lat.opp]
+        elif bc.kind == "extrapolation":
+            cs = extrapolation_cs(T)
+            miss = missing[:, m]
+            cells = np.array(np.nonzero(m))
+            nv = normals_float(lat, miss, T)
+            go = gout[:, m]
+            gp = gps[:, m]
+            for l in range(lat.q):
+                sel = miss[l]
+                if not sel.any():
+                    continue
+                src = cells[:, sel].copy()
+                for d in range(lat.d):
+                    src[d] = (src[d] - (lat.c[d, l] + nv[d, sel])) % shp[d]
+                g_aux = g0r[l][tuple(src)]
+                go[lat.opp[l], sel] = (T(1.0) - cs) * gp[l, sel] + cs * g_aux
+            gout[:, m] = go
+
+    f1_new = store.encode_deviation(gout)
+    skip = ids == 255
+    if skip.any():
+        f1_new[:, skip] = f1[:, skip]
     return _recovered(lat, f0, f1, bc_mask, missing, bcs), f1_new
 
 

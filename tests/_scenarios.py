@@ -116,8 +116,8 @@ class Scenario:
         pname, skind, T = POLICIES[policy]
         self.T = T
         self.omega = omega
-        # shifted FP16/BF16 policies run BGK in pair form (the stepper picks it)
-        self.collision = "BGK_PAIR" if (collision == "BGK" and pname in ("FP32FP16S", "FP32BF16S")) else collision
+        # shifted FP16/BF16 policies run BGK on the stored deviations (the stepper picks it)
+        self.collision = "BGK_SHIFTED" if (collision == "BGK" and pname in ("FP32FP16S", "FP32BF16S")) else collision
         self.lat = O.Lattice(lattice)
         self.store = O.Store(skind, self.lat)
         self.shape = tuple(shape)

@@ -102,3 +102,40 @@ def test_indices_masker_start_index_and_prior_marks():
     torch.cuda.synchronize()
     assert np.array_equal(bm.cpu().numpy(), want_bm)
     assert np.array_equal(mm.cpu().numpy(), want_mm)
+
+
+@pytest.mark.gpu
+def test_stepper_repacks_after_masker_writes():
+    """The stepper caches the packed missing bits against the mask tensors.  The
+    maskers write the masks through raw pointers, which torch does not see, so
+    they bump the tensors' version counters: a step after re-masking must use
+    the new marks, and another mask tensor (even one at a reused address) must
+    never hit the cache."""
+    import torch
+
+    import xlb_gb300 as xlb
+    from _scenarios import Scenario
+    from xlb_gb300.operator.boundary_condition import HalfwayBounceBackBC
+    from xlb_gb300.operator.boundary_masker import IndicesBoundaryMasker
+
+    sc = Scenario("D3Q19", (16, 12, 12), "channel_zouhe", policy="fp32")
+    f_0, f_1, bcm, mm = sc.gpu_fields()
+    f_0, f_1 = sc.stepper(f_0, f_1, bcm, mm, sc.omega, 0)
+    bits0 = sc.stepper._aux_state(bcm, mm)[0]
+    before = bits0.clone()
+
+    g = np.meshgrid(*[np.arange(s) for s in (16, 12, 12)], indexing="ij")
+    block = (g[0] >= 6) & (g[0] < 9) & (g[1] >= 4) & (g[1] < 7) & (g[2] >= 4) & (g[2] < 7)
+    idx = np.array([a[block] for a in g])
+    pp = xlb.PrecisionPolicy.FP32FP32
+    IndicesBoundaryMasker(xlb.velocity_set.D3Q19(pp), pp)([HalfwayBounceBackBC(indices=idx.tolist())], bcm, mm)
+    bits1 = sc.stepper._aux_state(bcm, mm)[0]
+    m = mm.cpu().numpy().reshape(19, -1).astype(np.int64)
+    want = np.bitwise_or.reduce(m << np.arange(19)[:, None], axis=0)
+    assert np.array_equal(bits1.cpu().numpy().astype(np.int64) & 0x7FFFF, want)
+    assert not torch.equal(bits1, before)
+
+    # a different mask tensor with other contents is packed afresh
+    mm2 = torch.zeros_like(mm)
+    bits2 = sc.stepper._aux_state(bcm, mm2)[0]
+    assert int(bits2.abs().sum()) == 0

@@ -154,14 +154,15 @@ def test_vector_kernel_skip_cells(policy):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("policy", ["fp32", "fp64", "f16"])
+@pytest.mark.parametrize("policy", ["fp32", "fp64", "f16", "f16s", "bf16s"])
 @pytest.mark.parametrize(
     "lattice,shape,layout",
     [("D2Q9", (30, 18), "channel_zouhe"), ("D3Q19", (16, 10, 10), "channel_regularized"),
      ("D3Q19", (6, 5, 136), "cavity_fullway"), ("D3Q27", (12, 10, 9), "cavity_halfway")],
 )
 def test_bgk_pair_form_matches_oracle(lattice, shape, layout, policy):
-    """collision_type="BGK_PAIR" under the XLB policies (the shifted policies use it by default)."""
+    """collision_type="BGK_PAIR" (pair form on f) under every policy; the shifted
+    policies default to BGK on the stored deviations instead."""
     sc = Scenario(lattice, shape, layout, policy=policy, collision="BGK_PAIR")
     sc.randomize(seed=9)
     want0, want1 = sc.oracle_steps(3)
@@ -200,27 +201,36 @@ def test_tma_staged_step_matches_oracle(lattice, shape, layout, policy):
     assert _lib.load().xlbg_device_faults(1) == 0
 
 
-@pytest.mark.gpu
-@pytest.mark.parametrize("env", [{"XLBG_WIDE_OFFSETS": "1"}, {"XLBG_TMA_X2": "1"}], ids=["wide", "tma_two_cell"])
-def test_kernel_variants_match_oracle(env):
-    """Kernel variants that the default dispatch does not select, forced in a
-    child process (the switches are read once per process): the marching
-    kernel's 64-bit plane offsets (used when Q x cells >= 2^32), and the
-    two-cell packed-arithmetic consumer of the TMA-staged step for pair-form
-    BGK with shifted 16-bit stores (the default there is one cell per
-    consumer)."""
-    import os
-    import subprocess
-    import sys
+VARIANT_CASES = [
+    ("D2Q9", (30, 18), "channel_regularized"),
+    ("D3Q19", (16, 10, 10), "channel_zouhe"),
+    ("D3Q19", (12, 10, 9), "cavity_fullway"),
+    ("D3Q27", (10, 8, 16), "channel_pressure"),
+    ("D3Q19", (6, 5, 264), "cavity_fullway"),
+    ("D3Q19", (10, 8, 16), "channel_regularized"),
+]
 
-    child_env = dict(os.environ, **env)
-    if "XLBG_TMA_X2" in env:
-        sel = "test_tma_staged_step_matches_oracle and (f16s or bf16s)"
-    else:
-        sel = ("(test_step_matches_oracle or test_store_forms_match_oracle) and "
-               "(channel_regularized or channel_zouhe or cavity_fullway)")
-    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-    r = subprocess.run([sys.executable, "-m", "pytest", os.path.abspath(__file__), "-q", "-x", "-m", "gpu", "-k", sel],
-                       env=child_env, capture_output=True, text=True, cwd=root)
-    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-2000:]
-    assert " passed" in r.stdout
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kernel", ["march", "march_wide", "cell", "tma_wide"])
+@pytest.mark.parametrize("policy", ["fp32", "f16s", "bf16s", "f16"])
+@pytest.mark.parametrize("lattice,shape,layout", VARIANT_CASES)
+def test_kernel_variants_match_oracle(lattice, shape, layout, policy, kernel):
+    """Kernel variants the automatic choice takes only on grids too large for a
+    test, or not on these shapes, forced through xlbg_debug_force_kernel: the
+    marching kernel with 32- and 64-bit plane offsets (64-bit when Q x cells >=
+    2^32, e.g. 1024 x 1024 x 768 D3Q19), the one-cell-per-thread kernel (grids
+    of 2^31 cells and more), and the TMA-staged kernel with 64-bit plane
+    offsets (the 16-bit stores on grids with Q x cells >= 2^32)."""
+    from xlb_gb300 import _lib
+
+    sel = {"march": _lib.KERNEL_MARCH, "march_wide": _lib.KERNEL_MARCH_WIDE, "cell": _lib.KERNEL_CELL,
+           "tma_wide": _lib.KERNEL_TMA_WIDE}[kernel]
+    sc = Scenario(lattice, shape, layout, policy=policy)
+    sc.randomize(seed=14)
+    want0, want1 = sc.oracle_steps(3)
+    with _lib.forced_kernel(sel):
+        got0, got1 = sc.gpu_steps(3)
+    _compare(got0, want0, "f_0")
+    _compare(got1, want1, "f_1")
+    assert _lib.load().xlbg_device_faults(1) == 0

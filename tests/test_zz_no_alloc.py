@@ -69,4 +69,9 @@ def test_noalloc_rejects_oversized_recovery_list():
                                             sc.omega, 0, -1, P(out), _lib.stream_handle())
     assert st == _lib.ERR_ARG
     assert b"exceeds" in _lib.load().xlbg_last_error()
+    # a count whose byte size overflows 64 bits is refused too, not wrapped into range
+    st = _lib.load().xlbg_step_diag_noalloc(sc.stepper.desc, P(f_0), P(f_1), P(bcm), P(bits), P(rec), 1 << 60,
+                                            sc.omega, 0, -1, P(out), _lib.stream_handle())
+    assert st == _lib.ERR_ARG
+    assert b"exceeds" in _lib.load().xlbg_last_error()
     assert ctypes.sizeof(ctypes.c_double) == 8

@@ -28,7 +28,9 @@ BC_REGULARIZED_VELOCITY = 6
 BC_REGULARIZED_PRESSURE = 7
 BC_EXTRAPOLATION = 8
 
-BGK, KBC, BGK_PAIR = 0, 1, 2
+BGK, KBC, BGK_PAIR, BGK_SHIFTED = 0, 1, 2, 3
+
+KERNEL_AUTO, KERNEL_MARCH, KERNEL_MARCH_WIDE, KERNEL_CELL, KERNEL_TMA_WIDE = 0, 1, 2, 3, 4
 
 MESH_TRI_FLOATS = 39
 MESH_EDGE_TESTS = 1
@@ -47,9 +49,11 @@ EXPORTED = (
     "xlbg_run",
     "xlbg_step_diag",
     "xlbg_step_diag_noalloc",
+    "xlbg_momentum_transfer",
     "xlbg_forward_segment",
     "xlbg_adjoint_segment",
     "xlbg_device_faults",
+    "xlbg_debug_force_kernel",
     "xlbg_equilibrium",
     "xlbg_macroscopic",
     "xlbg_indices_mask",
@@ -129,9 +133,11 @@ _SIGNATURES = {
     "xlbg_run": ([_DESC, _P, _P, _P, _P, _P, _I64, _P, _D, _I32, _I32, _P], ctypes.c_int),
     "xlbg_step_diag": ([_DESC, _P, _P, _P, _P, _P, _I64, _P, _D, _I32, _I32, _P, _P, _P], ctypes.c_int),
     "xlbg_step_diag_noalloc": ([_DESC, _P, _P, _P, _P, _P, _I64, _D, _I32, _I32, _P, _P], ctypes.c_int),
+    "xlbg_momentum_transfer": ([_DESC, _P, _P, _P, _I32, _P, _P, _P], ctypes.c_int),
     "xlbg_forward_segment": ([_DESC, _P, _I32, _P, _P, _P, _D, _P], ctypes.c_int),
     "xlbg_adjoint_segment": ([_DESC, _P, _I32, _P, _P, _P, _P, _I64, _P, _P, _P, _D, _P], ctypes.c_int),
     "xlbg_device_faults": ([_I32], ctypes.c_int),
+    "xlbg_debug_force_kernel": ([_I32], ctypes.c_int),
     "xlbg_equilibrium": ([_DESC, _P, _P, _D, ctypes.POINTER(_D), _P, _P], ctypes.c_int),
     "xlbg_macroscopic": ([_DESC, _P, _P, _P, _P], ctypes.c_int),
     "xlbg_indices_mask": ([_DESC, _P, _I64, _I32, _I32, _P, _P, _P], ctypes.c_int),
@@ -191,6 +197,34 @@ def lattice_tables(lattice):
 def ptr(t):
     """Device pointer of a torch tensor, or None."""
     return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def mark_written(*tensors):
+    """Bump the version counter of tensors a C-ABI call wrote in place.
+
+    Writes through raw pointers are invisible to torch; caches keyed on a
+    tensor's ``_version`` (the stepper's packed missing bits) see the change
+    only through this."""
+    import torch
+
+    for t in tensors:
+        if t is not None:
+            torch.autograd.graph.increment_version(t)
+
+
+class forced_kernel:
+    """Context manager: run the step entry points on one kernel variant
+    (KERNEL_*) inside the block, back to the automatic choice after it."""
+
+    def __init__(self, kernel):
+        self.kernel = kernel
+
+    def __enter__(self):
+        check(load().xlbg_debug_force_kernel(self.kernel))
+        return self
+
+    def __exit__(self, *exc):
+        check(load().xlbg_debug_force_kernel(KERNEL_AUTO))
 
 
 def stream_handle(stream=None):

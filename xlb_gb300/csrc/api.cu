@@ -7,6 +7,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 
+#include <atomic>
 #include <cmath>
 #include <string>
 
@@ -57,8 +58,11 @@ static int check_desc(const xlbg_desc* d) {
     return fail(XLBG_ERR_ARG, "unknown compute type %d", d->compute);
   if (d->compute == XLBG_COMPUTE_F64 && (d->store == XLBG_STORE_F16S || d->store == XLBG_STORE_BF16S))
     return fail(XLBG_ERR_UNSUPPORTED, "shifted FP16/BF16 storage is defined with FP32 compute only");
-  if (d->collision != XLBG_BGK && d->collision != XLBG_KBC && d->collision != XLBG_BGK_PAIR)
+  if (d->collision != XLBG_BGK && d->collision != XLBG_KBC && d->collision != XLBG_BGK_PAIR &&
+      d->collision != XLBG_BGK_SHIFTED)
     return fail(XLBG_ERR_ARG, "unknown collision %d", d->collision);
+  if (d->collision == XLBG_BGK_SHIFTED && d->store != XLBG_STORE_F16S && d->store != XLBG_STORE_BF16S)
+    return fail(XLBG_ERR_UNSUPPORTED, "BGK on stored deviations needs a shifted FP16/BF16 store");
   if (d->collision == XLBG_KBC && d->lattice == XLBG_D3Q19)
     return fail(XLBG_ERR_UNSUPPORTED, "KBC collision is defined for D2Q9 and D3Q27 only (kbc.py:184-185)");
   if (d->nx <= 0 || d->ny <= 0 || d->nz <= 0) return fail(XLBG_ERR_ARG, "grid shape must be positive");
@@ -77,6 +81,8 @@ static int check_desc(const xlbg_desc* d) {
   }
   return XLBG_OK;
 }
+
+int check_desc_public(const xlbg_desc* d) { return check_desc(d); }
 
 int check_ptr(const void* p, int align, const char* name) {
   if (!p) return fail(XLBG_ERR_ARG, "%s is NULL", name);
@@ -211,6 +217,12 @@ __global__ void diag_finalize_kernel(double* __restrict__ slots, double* __restr
   }
 }
 
+// The finaliser launched on its own (the standalone force operator).
+int launch_diag_finalize(double* slots, double* out, cudaStream_t s) {
+  diag_finalize_kernel<<<1, 1024, 0, s>>>(slots, out);
+  return (int)cudaGetLastError();
+}
+
 static unsigned grid_for(long long n, int block) {
   long long g = (n + block - 1) / block;
   if (g > 152LL * 64) g = 152LL * 64;
@@ -252,16 +264,8 @@ static void recovery_pass(const xlbg_desc* d, bool save, void* f, const int64_t*
     recovery_by_size<Lattice<2>>(bytes, save, f, cells, miss, scratch, nrec, n, s);
 }
 
-// XLBG_WIDE_OFFSETS=1 selects the 64-bit plane offsets of the marching kernel at
-// any size (they are needed only when Q * cells >= 2^32); lets small grids check
-// that instantiation against the oracle.
-static bool wide_forced() {
-  static const bool forced = [] {
-    const char* e = getenv("XLBG_WIDE_OFFSETS");
-    return e != nullptr && atoi(e) != 0;
-  }();
-  return forced;
-}
+// Kernel forced by xlbg_debug_force_kernel (XLBG_KERNEL_*); 0 = automatic.
+static std::atomic<int> g_force_kernel{XLBG_KERNEL_AUTO};
 
 int fill_step_args(const xlbg_desc* d, const void* f0, void* f1, const uint8_t* bc_mask,
                           const uint32_t* miss, double omega, StepArgs& a) {
@@ -271,7 +275,9 @@ int fill_step_args(const xlbg_desc* d, const void* f0, void* f1, const uint8_t* 
   a.bc_mask = bc_mask;
   a.miss = miss;
   a.ncell = ncells(d);
-  a.wide = wide_forced() || (long long)lattice_q(d->lattice) * a.ncell > 0xffffffffLL;
+  const int force = g_force_kernel.load();
+  a.wide = force == XLBG_KERNEL_MARCH_WIDE || force == XLBG_KERNEL_TMA_WIDE ||
+           (long long)lattice_q(d->lattice) * a.ncell > 0xffffffffLL;
   internal_dims(d, a.n0, a.n1, a.n2);
   a.nbc = d->nbc;
   a.omega = omega;
@@ -299,15 +305,9 @@ int fill_step_args(const xlbg_desc* d, const void* f0, void* f1, const uint8_t* 
   return XLBG_OK;
 }
 
-// Rows per thread of the marching kernel.  XLBG_CHUNK overrides it (0 selects
-// the one-cell-per-thread kernel); the default keeps at least eight blocks per
-// SM of a 152-SM GB300 and at most 64 rows per thread.
+// Rows per thread of the marching kernel: at least eight blocks per SM of a
+// 152-SM GB300 and at most 64 rows per thread.
 static int choose_chunk(const StepArgs& a, int threads) {
-  static const int forced = [] {
-    const char* e = getenv("XLBG_CHUNK");
-    return e ? atoi(e) : -1;
-  }();
-  if (forced >= 0) return forced;
   const long long columns = (long long)a.n0 * ((a.n2 + threads - 1) / threads);
   long long chunk = (long long)a.n1 * columns / (152LL * 8);
   if (chunk < 1) chunk = 1;
@@ -319,13 +319,16 @@ int try_launch_tma(const xlbg_desc* d, const StepArgs& a, bool fullbc, bool diag
 
 int launch_main(const xlbg_desc* d, const StepArgs& a, bool diag, cudaStream_t s) {
   const bool full = needs_full_bc(d) || diag;
+  const int force = g_force_kernel.load();
   // 16-bit stores: TMA-staged rows when the shape allows (1 = not applicable)
-  const int t = try_launch_tma(d, a, full, diag, s);
-  if (t != 1) return t;
-  const bool pair = d->collision == XLBG_BGK_PAIR;
+  if (force == XLBG_KERNEL_AUTO || force == XLBG_KERNEL_TMA_WIDE) {
+    const int t = try_launch_tma(d, a, full, diag, s);
+    if (t != 1) return t;
+  }
+  const int pair = d->collision == XLBG_KBC ? 0 : d->collision;  // BGK form: 0, 2 or 3
   int r = -1;
   // the marching kernel keeps cell offsets in 32 bits (plane offsets are 64-bit when a.wide)
-  if (a.ncell < 0x7fffffffLL) {
+  if (a.ncell < 0x7fffffffLL && force != XLBG_KERNEL_CELL) {
     const int threads = a.n2 >= kStepBlock ? kStepBlock : ((a.n2 + 31) / 32) * 32;
     const int chunk = choose_chunk(a, threads);
     if (chunk > 0) {
@@ -452,6 +455,13 @@ using namespace xlbg;
 extern "C" {
 
 int xlbg_abi_version(void) { return XLBG_ABI_VERSION; }
+
+int xlbg_debug_force_kernel(int32_t kernel) {
+  if (kernel < XLBG_KERNEL_AUTO || kernel > XLBG_KERNEL_TMA_WIDE)
+    return fail(XLBG_ERR_ARG, "unknown kernel selector %d", kernel);
+  g_force_kernel.store(kernel);
+  return XLBG_OK;
+}
 
 const char* xlbg_last_error(void) { return g_last_error.c_str(); }
 

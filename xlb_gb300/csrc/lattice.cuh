@@ -84,6 +84,14 @@ __host__ __device__ constexpr double weight(int l) {
                                  : (norm1<L>(l) == 1 ? 2.0 / 27.0 : (norm1<L>(l) == 2 ? 1.0 / 54.0 : 1.0 / 216.0)));
 }
 
+// Weight of the directions with |c|_1 = k (0 when the lattice has none).
+template <class L>
+__host__ __device__ constexpr double class_weight(int k) {
+  for (int l = 0; l < L::Q; ++l)
+    if (norm1<L>(l) == k) return weight<L>(l);
+  return 0.0;
+}
+
 template <class L>
 __host__ __device__ constexpr int opp(int l) {
   return L::opp(l);

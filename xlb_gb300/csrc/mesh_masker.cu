@@ -149,9 +149,14 @@ __global__ void mesh_solid(const float* __restrict__ rec, long long n_tri, const
   int p0[3], p1[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    // voxel p has box [p - 1, p]: the bounds [lo, hi] meet it iff ceil(lo) <= p <= floor(hi) + 1
-    p0[k] = max((int)ceilf(r[k]), bo[k]);
-    p1[k] = min(min((int)floorf(r[3 + k]) + 1, bo[k] + brick - 1), pd[k] - 1);
+    // voxel p has box [p - 1, p]: the bounds [lo, hi] meet it iff ceil(lo) <= p <= floor(hi) + 1.
+    // Clamped to the brick in float before converting, so coordinates far outside
+    // the grid (or not finite: every comparison with NaN is false) cannot overflow.
+    const float lo = ceilf(r[k]), hi = floorf(r[3 + k]) + 1.0f;
+    const float lim0 = (float)bo[k], lim1 = (float)min(bo[k] + brick - 1, pd[k] - 1);
+    if (!(lo <= lim1 && hi >= lim0)) return;  // the bounds miss this brick
+    p0[k] = (int)fmaxf(lo, lim0);
+    p1[k] = (int)fminf(hi, lim1);
   }
   for (int i = p0[0]; i <= p1[0]; ++i)
     for (int j = p0[1]; j <= p1[1]; ++j)

@@ -20,6 +20,7 @@
 #include <mutex>
 
 #include "../../include/xlbg.h"
+#include "ctx.cuh"
 #include "step_dispatch.cuh"
 
 namespace xlbg {
@@ -43,14 +44,17 @@ constexpr int kMaxDevices = 64;
 struct NoallocPtrs {
   double* slots = nullptr;
   void* rec = nullptr;
+  void* ctx = nullptr;  // context the addresses belong to
   bool ready = false;
 };
 std::mutex g_noalloc_mu;
 NoallocPtrs g_noalloc_ptrs[kMaxDevices];
 
-// Device addresses of the static arrays for the current device, looked up once
-// per device.  In host code the array names are host-side stand-ins, never
-// device addresses; only cudaGetSymbolAddress yields the real ones.
+// Device addresses of the static arrays for the current device.  In host code
+// the array names are host-side stand-ins, never device addresses; only
+// cudaGetSymbolAddress yields the real ones.  They are looked up on the first
+// call on a device (with that device current) and again whenever the device's
+// context has changed since (cudaDeviceReset gives it a new one).
 int noalloc_pointers(NoallocPtrs& out) {
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
@@ -58,7 +62,8 @@ int noalloc_pointers(NoallocPtrs& out) {
   if (dev < 0 || dev >= kMaxDevices) return fail(XLBG_ERR_ARG, "device ordinal %d outside 0..%d", dev, kMaxDevices - 1);
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
   NoallocPtrs& p = g_noalloc_ptrs[dev];
-  if (!p.ready) {
+  void* ctx = current_context();
+  if (!p.ready || ctx == nullptr || ctx != p.ctx) {
     void* slots = nullptr;
     void* rec = nullptr;
     e = cudaGetSymbolAddress(&slots, g_noalloc_diag_slots);
@@ -67,6 +72,7 @@ int noalloc_pointers(NoallocPtrs& out) {
     if (e != cudaSuccess) return fail(XLBG_ERR_CUDA, "cudaGetSymbolAddress(recovery scratch): %s", cudaGetErrorString(e));
     p.slots = static_cast<double*>(slots);
     p.rec = rec;
+    p.ctx = current_context();  // the lookup made the primary context current if it was not
     p.ready = true;
   }
   out = p;
@@ -88,12 +94,14 @@ extern "C" int xlbg_step_diag_noalloc(const xlbg_desc* d, void* f0, void* f1, co
   if ((e = check_step_args(d, f0, f1, bc_mask, miss, rec_cells, n_rec, p.rec))) return e;
   if ((e = check_ptr(diag, 8, "diag"))) return e;
   const int q = d->lattice == XLBG_D2Q9 ? 9 : (d->lattice == XLBG_D3Q19 ? 19 : 27);
-  const long long need = (long long)n_rec * q * store_bytes(d->store);
-  if (need > (long long)XLBG_NOALLOC_REC_SCRATCH_BYTES)
+  // compared by division: n_rec * q * bytes could overflow for a bogus n_rec
+  const long long per_cell = (long long)q * store_bytes(d->store);
+  if (n_rec > (long long)XLBG_NOALLOC_REC_SCRATCH_BYTES / per_cell)
     return fail(XLBG_ERR_ARG,
-                "xlbg_step_diag_noalloc: %lld recovery cells x %d directions x %d bytes = %lld bytes exceeds the "
-                "%u-byte static scratch; use xlbg_step_diag with caller scratch",
-                (long long)n_rec, q, store_bytes(d->store), need, (unsigned)XLBG_NOALLOC_REC_SCRATCH_BYTES);
+                "xlbg_step_diag_noalloc: %lld recovery cells x %d directions x %d bytes exceeds the "
+                "%u-byte static scratch (at most %lld cells); use xlbg_step_diag with caller scratch",
+                (long long)n_rec, q, store_bytes(d->store), (unsigned)XLBG_NOALLOC_REC_SCRATCH_BYTES,
+                (long long)XLBG_NOALLOC_REC_SCRATCH_BYTES / per_cell);
   cudaStream_t s = (cudaStream_t)stream;
   // The slots keep the previous call's contents; the reduction needs them zero.
   cudaError_t ce = cudaMemsetAsync(p.slots, 0, sizeof(double) * XLBG_DIAG_SLOTS * 4, s);

@@ -219,6 +219,86 @@ __device__ __forceinline__ void bgk_pair(const T (&f)[L::Q], T omega, T (&fo)[L:
   pair_update<L, T, 0>(f, u, base, omf, orho, fo);
 }
 
+// BGK on the stored deviations of the shifted FP16 / BF16 forms (collision
+// code 3; no XLB counterpart).  The same equations as macroscopic + quadratic
+// equilibrium + BGK (bgk.py:30-34, quadratic_equilibrium.py:35-60), written
+// for g_l = S (f_l - w_l) as the store holds it (S = 2^14 for FP16S, 1 for
+// BF16S) so that a pulled value is one conversion from its bits and a result
+// one conversion to them, and no FP32 rounding of f ~ w is paid on top of the
+// 16-bit one:
+//   rho = 1 + G / S,  u = J / (S rho),   G = sum_l g_l,  J = sum_l c_l g_l,
+//   S (feq_l - w_l) = S w_l (rho e_l - 1),  e_l = 1 + t + t^2 / 2 - 1.5 |u|^2,  t = 3 c_l.u,
+//   g_out = (1 - omega) g + omega S (feq - w).
+// Over an opposite pair (l, o) t changes sign; with A = omega S w (one per
+// weight class), v = 3u, base = 1 - |v|^2 / 6, C = A rho base - A (one fused
+// multiply-add per class) and R = C + (A rho / 2) t^2:
+//   g_out_l = fma(1 - omega, g_l, fma( A rho, t, R)),
+//   g_out_o = fma(1 - omega, g_o, fma(-A rho, t, R)).
+// About 125 floating-point operations per D3Q19 cell, decode and encode
+// included, against about 200 for the pair form on f.
+template <int SK>
+__host__ __device__ constexpr float shift_scale() {
+  return SK == 3 ? 16384.0f : 1.0f;  // SK_F16S : SK_BF16S
+}
+
+template <class L, int P>
+__device__ __forceinline__ void shifted_pair_update(const float (&g)[L::Q], const float (&v)[L::D],
+                                                    const float (&Ar)[4], const float (&Arh)[4], const float (&C)[4],
+                                                    float omf, float (&go)[L::Q]) {
+  if constexpr (P < (L::Q - 1) / 2) {
+    constexpr int l = pair_at<L>(P);
+    constexpr int o = opp<L>(l);
+    constexpr int k = norm1<L>(l);
+    float t = 0.0f;
+    bool first = true;
+#pragma unroll
+    for (int d = 0; d < L::D; ++d) {
+      if (L::c(l, d) != 0) {
+        const float x = L::c(l, d) == 1 ? v[d] : -v[d];
+        t = first ? x : t + x;
+        first = false;
+      }
+    }
+    const float q = Arh[k] * t;
+    const float R = __fmaf_rn(q, t, C[k]);
+    go[l] = __fmaf_rn(omf, g[l], __fmaf_rn(Ar[k], t, R));
+    go[o] = __fmaf_rn(omf, g[o], __fmaf_rn(-Ar[k], t, R));
+    shifted_pair_update<L, P + 1>(g, v, Ar, Arh, C, omf, go);
+  }
+}
+
+template <class L, int SK>
+__device__ __forceinline__ void bgk_shifted(const float (&g)[L::Q], float omega, float (&go)[L::Q]) {
+  constexpr float S = shift_scale<SK>();
+  constexpr float K = 1.0f / S;  // a power of two: exact
+  float G = g[0];
+  float J[L::D];
+#pragma unroll
+  for (int d = 0; d < L::D; ++d) J[d] = 0.0f;
+  pair_moments<L, float, 0>(g, G, J);
+  const float rho = __fmaf_rn(K, G, 1.0f);
+  const float k3 = 3.0f * (K * __frcp_rn(rho));
+  float v[L::D];
+#pragma unroll
+  for (int d = 0; d < L::D; ++d) v[d] = J[d] * k3;
+  float vsq = v[0] * v[0];
+#pragma unroll
+  for (int d = 1; d < L::D; ++d) vsq = __fmaf_rn(v[d], v[d], vsq);
+  const float base = __fmaf_rn(-1.0f / 6.0f, vsq, 1.0f);
+  const float omf = 1.0f - omega;
+  float Ar[4] = {0.0f, 0.0f, 0.0f, 0.0f}, Arh[4] = {0.0f, 0.0f, 0.0f, 0.0f}, C[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+  for (int k = 0; k <= L::D; ++k) {
+    // weight class |c|_1 = k (D2Q9 and D3Q19 have no k = 3; the unused entries fold away)
+    const float A = omega * (S * (float)class_weight<L>(k));
+    Ar[k] = A * rho;
+    Arh[k] = 0.5f * Ar[k];
+    C[k] = __fmaf_rn(Ar[k], base, -A);
+  }
+  go[0] = __fmaf_rn(omf, g[0], C[0]);
+  shifted_pair_update<L, 0>(g, v, Ar, Arh, C, omf, go);
+}
+
 // -c of the first missing direction with |c|_1 = 1 (helper_functions_bc.py:250-261,
 // bc_extrapolation_outflow.py:358-369).  Zero when there is none.
 template <class L>

@@ -1,9 +1,9 @@
 // Fused step kernels (one cell per thread) for D3Q19 with BGK collision, in XLB's
-// operation order (collision code 0) and in pair form (collision code 2).
+// operation order (collision code 0), in pair form (code 2) and on stored deviations (code 3).
 #include "step_dispatch.cuh"
 
 namespace xlbg {
-int launch_step_d3q19_bgk(const StepArgs& a, int sk, int compute, bool fullbc, bool diag, bool pair, cudaStream_t s) {
-  return pair ? launch_step_t<1, 2>(a, sk, compute, fullbc, diag, s) : launch_step_t<1, 0>(a, sk, compute, fullbc, diag, s);
+int launch_step_d3q19_bgk(const StepArgs& a, int sk, int compute, bool fullbc, bool diag, int form, cudaStream_t s) {
+  return XLBG_BGK_FORM(launch_step_t, 1, a, sk, compute, fullbc, diag, s);
 }
 }  // namespace xlbg

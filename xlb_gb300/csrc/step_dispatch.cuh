@@ -8,6 +8,9 @@
 namespace xlbg {
 
 // Returns 0 on launch, -1 for an unsupported store/compute pair, or the CUDA error.
+// Pick the instantiation of a BGK form (0, 2 or 3) at run time.
+#define XLBG_BGK_FORM(FN, LAT, ...) \
+  (form == 3 ? FN<LAT, 3>(__VA_ARGS__) : form == 2 ? FN<LAT, 2>(__VA_ARGS__) : FN<LAT, 0>(__VA_ARGS__))
 template <int LAT, int COLL>
 int launch_step_t(const StepArgs& a, int sk, int compute, bool fullbc, bool diag, cudaStream_t s) {
   using L = Lattice<LAT>;
@@ -21,7 +24,14 @@ int launch_step_t(const StepArgs& a, int sk, int compute, bool fullbc, bool diag
     else                                                                             \
       step_kernel<L, SKV, TV, COLL, false, false><<<grid, kStepBlock, 0, s>>>(a);   \
   } while (0)
-  if (compute == 1) {
+  if constexpr (COLL == 3) {  // stored deviations: shifted stores, FP32 compute only
+    if (compute == 1) return -1;
+    switch (sk) {
+      case SK_F16S: XLBG_LAUNCH(SK_F16S, float); break;
+      case SK_BF16S: XLBG_LAUNCH(SK_BF16S, float); break;
+      default: return -1;
+    }
+  } else if (compute == 1) {
     switch (sk) {
       case SK_F64: XLBG_LAUNCH(SK_F64, double); break;
       case SK_F32: XLBG_LAUNCH(SK_F32, double); break;
@@ -69,7 +79,14 @@ int launch_step_march_t(const StepArgs& a, int sk, int compute, bool fullbc, int
   const int zblocks = (a.n2 + threads - 1) / threads;
   const dim3 grid((unsigned)(a.n0 * zblocks), (unsigned)((a.n1 + chunk - 1) / chunk));
 #define XLBG_MLAUNCH(SKV, TV) launch_march_variant<L, SKV, TV, COLL>(a, fullbc, grid, threads, chunk, s)
-  if (compute == 1) {
+  if constexpr (COLL == 3) {  // stored deviations: shifted stores, FP32 compute only
+    if (compute == 1) return -1;
+    switch (sk) {
+      case SK_F16S: XLBG_MLAUNCH(SK_F16S, float); break;
+      case SK_BF16S: XLBG_MLAUNCH(SK_BF16S, float); break;
+      default: return -1;
+    }
+  } else if (compute == 1) {
     switch (sk) {
       case SK_F64: XLBG_MLAUNCH(SK_F64, double); break;
       case SK_F32: XLBG_MLAUNCH(SK_F32, double); break;
@@ -89,16 +106,17 @@ int launch_step_march_t(const StepArgs& a, int sk, int compute, bool fullbc, int
   return (int)cudaGetLastError();
 }
 
-int launch_step_march_d2q9_bgk(const StepArgs&, int, int, bool, bool, int, int, cudaStream_t);
+// BGK launchers take the BGK form: 0 (XLB order), 2 (pair form) or 3 (stored deviations).
+int launch_step_march_d2q9_bgk(const StepArgs&, int, int, bool, int, int, int, cudaStream_t);
 int launch_step_march_d2q9_kbc(const StepArgs&, int, int, bool, int, int, cudaStream_t);
-int launch_step_march_d3q19_bgk(const StepArgs&, int, int, bool, bool, int, int, cudaStream_t);
-int launch_step_march_d3q27_bgk(const StepArgs&, int, int, bool, bool, int, int, cudaStream_t);
+int launch_step_march_d3q19_bgk(const StepArgs&, int, int, bool, int, int, int, cudaStream_t);
+int launch_step_march_d3q27_bgk(const StepArgs&, int, int, bool, int, int, int, cudaStream_t);
 int launch_step_march_d3q27_kbc(const StepArgs&, int, int, bool, int, int, cudaStream_t);
 
-int launch_step_d2q9_bgk(const StepArgs&, int, int, bool, bool, bool, cudaStream_t);
+int launch_step_d2q9_bgk(const StepArgs&, int, int, bool, bool, int, cudaStream_t);
 int launch_step_d2q9_kbc(const StepArgs&, int, int, bool, bool, cudaStream_t);
-int launch_step_d3q19_bgk(const StepArgs&, int, int, bool, bool, bool, cudaStream_t);
-int launch_step_d3q27_bgk(const StepArgs&, int, int, bool, bool, bool, cudaStream_t);
+int launch_step_d3q19_bgk(const StepArgs&, int, int, bool, bool, int, cudaStream_t);
+int launch_step_d3q27_bgk(const StepArgs&, int, int, bool, bool, int, cudaStream_t);
 int launch_step_d3q27_kbc(const StepArgs&, int, int, bool, bool, cudaStream_t);
 
 }  // namespace xlbg

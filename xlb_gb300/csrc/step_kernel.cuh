@@ -118,7 +118,8 @@ __device__ __forceinline__ int wrap_inc(int i, int n) { return i == n - 1 ? 0 : 
 
 // Pull stream for one cell: f[l] = f0[l, x - c_l] with XLB's one-cell periodic
 // wrap (stream.py:64-82).
-template <class L, int SK, class T>
+// With collision code 3 the values are the stored deviations (load_pop).
+template <class L, int SK, class T, int COLL>
 __device__ __forceinline__ void pull_cell(const StepArgs& a, int i0, int i1, int i2, T (&f)[L::Q]) {
   using St = Store<SK, T>;
   using Bits = typename St::Bits;
@@ -127,14 +128,17 @@ __device__ __forceinline__ void pull_cell(const StepArgs& a, int i0, int i1, int
   const int z[3] = {i2 == n2 - 1 ? 0 : i2 + 1, i2, i2 == 0 ? n2 - 1 : i2 - 1};  // source i2 for c2 = -1, 0, +1
 #pragma unroll
   for (int l = 0; l < L::Q; ++l) {
-    f[l] = St::dec(ldg_bits(at0<Bits>(a, l, rows.of<L>(l) + z[axis_c<L>(l, 2) + 1])), T(weight<L>(l)));
+    f[l] = load_pop<SK, T, COLL>(ldg_bits(at0<Bits>(a, l, rows.of<L>(l) + z[axis_c<L>(l, 2) + 1])), T(weight<L>(l)));
   }
 }
 
-// Collision of one cell: XLB-order BGK (COLL 0), KBC (COLL 1) or pair-form BGK (COLL 2).
-template <class L, class T, int COLL>
+// Collision of one cell: XLB-order BGK (COLL 0), KBC (COLL 1), pair-form BGK
+// (COLL 2) or BGK on the stored deviations of the shifted stores (COLL 3).
+template <class L, int SK, class T, int COLL>
 __device__ __forceinline__ void collide(const T (&f)[L::Q], T omega, T (&fo)[L::Q]) {
-  if constexpr (COLL == 2) {
+  if constexpr (COLL == 3) {
+    bgk_shifted<L, SK>(f, omega, fo);
+  } else if constexpr (COLL == 2) {
     bgk_pair<L>(f, omega, fo);
   } else {
     T rho, u[L::D];
@@ -152,7 +156,7 @@ __device__ __forceinline__ void collide(const T (&f)[L::Q], T omega, T (&fo)[L::
 
 // Store of one cell's post-collision populations (nse_stepper.py:379-381); with
 // DIAG, the cell's mass as stored, summed in T.
-template <class L, int SK, class T, bool DIAG, class Idx>
+template <class L, int SK, class T, int COLL, bool DIAG, class Idx>
 __device__ __forceinline__ void store_cell(const StepArgs& a, Idx cell, const T (&fo)[L::Q], double& dmass) {
   using St = Store<SK, T>;
   using Bits = typename St::Bits;
@@ -164,7 +168,7 @@ __device__ __forceinline__ void store_cell(const StepArgs& a, Idx cell, const T 
   const size_t plane = (size_t)a.ncell;
 #pragma unroll
   for (int l = 0; l < L::Q; ++l) {
-    const Bits b = St::enc(fo[l], T(weight<L>(l)));
+    const Bits b = store_pop<SK, T, COLL>(fo[l], T(weight<L>(l)));
     if constexpr (sizeof(Bits) == 2)
       row1[(size_t)l * plane] = b;
     else
@@ -180,6 +184,10 @@ __device__ __forceinline__ void store_cell(const StepArgs& a, Idx cell, const T 
 // Everything after the pull for one cell: BC lookup, streaming-step BC,
 // collision, collision-step BC, store to f1 and the diagnostics contributions.
 // f holds the pulled values of the cell; the cell is not a skip cell (id 255).
+// With collision code 3 every value in f and fo is a stored deviation g: the
+// bounce-back kinds copy deviations (w_l = w_opp l), the extrapolation blend is
+// linear, and EquilibriumBC / ZouHe / Regularized run in f (XLB's order) between
+// one from_dev / to_dev per direction.
 // The collision is inlined once, shared by fluid and boundary cells (a second
 // copy for a fluid-only path doubled the code and ran slower).
 template <class L, int SK, class T, int COLL, bool FULLBC, bool DIAG, class Idx>
@@ -214,7 +222,7 @@ __device__ __forceinline__ void cell_update(const StepArgs& a, int i0, int i1, i
 #pragma unroll
       for (int l = 0; l < Q; ++l) {
         if ((miss >> l) & 1u)
-          f[l] = St::dec(ldg_bits(at0<Bits>(a, opp<L>(l), cell)), T(weight<L>(opp<L>(l))));
+          f[l] = load_pop<SK, T, COLL>(ldg_bits(at0<Bits>(a, opp<L>(l), cell)), T(weight<L>(opp<L>(l))));
       }
     } else if (kind == BC_EQUILIBRIUM) {
       // bc_equilibrium.py:255-271
@@ -222,16 +230,28 @@ __device__ __forceinline__ void cell_update(const StepArgs& a, int i0, int i1, i
 #pragma unroll
       for (int d = 0; d < L::D; ++d) u[d] = T(bc_u[d]);
       equilibrium<L>(T(bc_rho), u, f);
+      if constexpr (COLL == 3) {
+#pragma unroll
+        for (int l = 0; l < Q; ++l) f[l] = St::to_dev(f[l], T(weight<L>(l)));
+      }
     } else if (FULLBC && kind >= BC_ZOUHE_V && kind <= BC_REG_P) {
       // the prescribed value lives in slot 0 of f1 (boundary_condition.py:151-152)
       const T aux = St::dec_raw(static_cast<const Bits*>(a.aux)[cell]);
+      if constexpr (COLL == 3) {
+#pragma unroll
+        for (int l = 0; l < Q; ++l) f[l] = St::from_dev(f[l], T(weight<L>(l)));
+      }
       zouhe_like<L>(f, miss, aux, kind);
+      if constexpr (COLL == 3) {
+#pragma unroll
+        for (int l = 0; l < Q; ++l) f[l] = St::to_dev(f[l], T(weight<L>(l)));
+      }
     }
   }
 
   // ---- macroscopic, equilibrium, collision ----
   T fo[Q];
-  collide<L, T, COLL>(f, omega_of<T>(a), fo);
+  collide<L, SK, T, COLL>(f, omega_of<T>(a), fo);
 
   // ---- collision-step BCs ----
   if (kind == BC_FULLWAY) {
@@ -255,13 +275,13 @@ __device__ __forceinline__ void cell_update(const StepArgs& a, int i0, int i1, i
         const int s1 = wrap_any(i1 - (axis_c<L>(l, 1) + m1), n1);
         const int s2 = wrap_any(i2 - (axis_c<L>(l, 2) + m2), n2);
         const long long src = ((long long)s0 * n1 + s1) * n2 + s2;
-        const T faux = St::dec(ldg_bits(at0<Bits>(a, l, (Idx)src)), T(weight<L>(l)));
+        const T faux = load_pop<SK, T, COLL>(ldg_bits(at0<Bits>(a, l, (Idx)src)), T(weight<L>(l)));
         fo[opp<L>(l)] = (T(1) - cs) * f[l] + cs * faux;
       }
     }
   }
 
-  store_cell<L, SK, T, DIAG>(a, cell, fo, dmass);
+  store_cell<L, SK, T, COLL, DIAG>(a, cell, fo, dmass);
   if constexpr (DIAG) {
     if ((int)id == a.force_id && !(miss & 1u)) {
       // momentum exchange on the input state (momentum_transfer.py:130-158):
@@ -338,7 +358,7 @@ __global__ void __launch_bounds__(kStepBlock) step_kernel(const StepArgs a) {
   const uint8_t id = inside ? a.bc_mask[cell] : (uint8_t)255;
   if (id != 255) {
     T f[Q];
-    pull_cell<L, SK, T>(a, i0, i1, i2, f);
+    pull_cell<L, SK, T, COLL>(a, i0, i1, i2, f);
     cell_update<L, SK, T, COLL, FULLBC, DIAG>(a, i0, i1, i2, cell, id, f, dmass, dforce);
   }
   if constexpr (DIAG) reduce_diag(dmass, dforce, a.diag_slots);
@@ -405,7 +425,7 @@ __global__ void __launch_bounds__(kStepBlock, march_min_blocks<L, T>()) step_ker
 #pragma unroll
     for (int l = 0; l < Q; ++l) {
       const unsigned src = xz[axis_c<L>(l, 0) + 1][axis_c<L>(l, 2) + 1] + yo[axis_c<L>(l, 1) + 1];
-      f[l] = St::dec(ldg_bits(at0<Bits>(a, l, (Idx)src)), T(weight<L>(l)));
+      f[l] = load_pop<SK, T, COLL>(ldg_bits(at0<Bits>(a, l, (Idx)src)), T(weight<L>(l)));
     }
     if constexpr (DIAG) {
       double dmc = 0.0, dfc[3] = {0.0, 0.0, 0.0};

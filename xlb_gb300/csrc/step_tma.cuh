@@ -27,6 +27,8 @@
 #include <cuda.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "step_kernel.cuh"
 
 namespace xlbg {
@@ -165,8 +167,11 @@ __device__ __forceinline__ void tma_produce(const CUtensorMap& map, unsigned bas
 // with box = min(n2, 256).  Grid: (n0, ceil(n1 / rows)); CT + 32 threads per
 // block, CT = tma_consumers<PITCH>(): CT consumers (thread i2 owns cell i2 of
 // every row) and one producer warp, whose lanes issue the copies.  Staged rows
-// hold PITCH elements; n2 <= CT, n2 % 8 == 0; cell and plane offsets fit 32 bits
-// (the host checks).
+// hold PITCH elements; n2 <= CT, n2 % 8 == 0; cell offsets fit 31 bits (the host
+// checks).  Plane offsets: the fluid path stores through the cell's slot in
+// plane 0 plus 64-bit plane offsets at any size; the boundary paths index
+// f0 / f1 planes with Idx, 32-bit unsigned when Q * cells < 2^32 and 64-bit
+// (WIDE) above, e.g. for 1024 x 1024 x 768 cells.
 //
 // Hand-off per stage s (row k, use u = k / S):
 //   producer: wait empty[s] phase u - 1 (u > 0); lane 0 posts expect_tx on
@@ -174,10 +179,11 @@ __device__ __forceinline__ void tma_produce(const CUtensorMap& map, unsigned bas
 //   consumer warp: wait full[s] phase u, read its cells, __syncwarp, lane 0
 //                  arrives on empty[s] (CT / 32 arrivals complete the phase)
 // No block-wide barrier after set-up: consumer warps drift up to S rows apart.
-template <class L, int SK, int COLL, bool FULLBC, int PITCH>
+template <class L, int SK, int COLL, bool FULLBC, int PITCH, bool WIDE>
 __global__ void __launch_bounds__(tma_consumers<PITCH>() + 32, tma_min_blocks<PITCH>())
     step_kernel_tma(const __grid_constant__ CUtensorMap map, const StepArgs a, int rows, int box, int* err) {
   using T = float;
+  using Idx = typename std::conditional<WIDE, long long, unsigned>::type;
   using St = Store<SK, T>;
   using Bits = typename St::Bits;
   static_assert(sizeof(Bits) == 2, "16-bit stores only");
@@ -241,31 +247,41 @@ __global__ void __launch_bounds__(tma_consumers<PITCH>() + 32, tma_min_blocks<PI
       const unsigned char* st = smem + s * STAGE;
 #pragma unroll
       for (int l = 0; l < Q; ++l)
-        f[l] = St::dec(*reinterpret_cast<const Bits*>(st + l * ROW + zb[axis_c<L>(l, 2) + 1]), T(weight<L>(l)));
+        f[l] = load_pop<SK, T, COLL>(*reinterpret_cast<const Bits*>(st + l * ROW + zb[axis_c<L>(l, 2) + 1]),
+                                     T(weight<L>(l)));
     }
     __syncwarp();
     if (lane == 0) mbar_arrive(empty + 8 * s);
-    if (id != 255) cell_update<L, SK, T, COLL, FULLBC, false>(a, i0, y, i2, cell, id, f, dm, df);
+    if (id != 255) cell_update<L, SK, T, COLL, FULLBC, false>(a, i0, y, i2, (Idx)cell, id, f, dm, df);
   }
 }
 
 // Launch for one (lattice, store, collision): picks the pitch, sets the shared
 // memory size once per instantiation.  Returns the CUDA error of the launch.
-template <class L, int SK, int COLL, int PITCH>
-int launch_tma_pitch(const CUtensorMap& map, const StepArgs& a, bool fullbc, int rows, int box, int* err,
-                     cudaStream_t s) {
+template <class L, int SK, int COLL, int PITCH, bool WIDE>
+int launch_tma_variant(const CUtensorMap& map, const StepArgs& a, bool fullbc, int rows, int box, int* err,
+                       cudaStream_t s) {
   const unsigned smem = tma_smem_bytes<L, PITCH>();
-  static const bool attr_full = cudaFuncSetAttribute(step_kernel_tma<L, SK, COLL, true, PITCH>,
+  static const bool attr_full = cudaFuncSetAttribute(step_kernel_tma<L, SK, COLL, true, PITCH, WIDE>,
                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, smem) == cudaSuccess;
-  static const bool attr_part = cudaFuncSetAttribute(step_kernel_tma<L, SK, COLL, false, PITCH>,
+  static const bool attr_part = cudaFuncSetAttribute(step_kernel_tma<L, SK, COLL, false, PITCH, WIDE>,
                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, smem) == cudaSuccess;
   if (!attr_full || !attr_part) return (int)cudaErrorInvalidValue;
   const dim3 grid((unsigned)a.n0, (unsigned)((a.n1 + rows - 1) / rows));
   if (fullbc)
-    step_kernel_tma<L, SK, COLL, true, PITCH><<<grid, tma_consumers<PITCH>() + 32, smem, s>>>(map, a, rows, box, err);
+    step_kernel_tma<L, SK, COLL, true, PITCH, WIDE>
+        <<<grid, tma_consumers<PITCH>() + 32, smem, s>>>(map, a, rows, box, err);
   else
-    step_kernel_tma<L, SK, COLL, false, PITCH><<<grid, tma_consumers<PITCH>() + 32, smem, s>>>(map, a, rows, box, err);
+    step_kernel_tma<L, SK, COLL, false, PITCH, WIDE>
+        <<<grid, tma_consumers<PITCH>() + 32, smem, s>>>(map, a, rows, box, err);
   return (int)cudaGetLastError();
+}
+
+template <class L, int SK, int COLL, int PITCH>
+int launch_tma_pitch(const CUtensorMap& map, const StepArgs& a, bool fullbc, int rows, int box, int* err,
+                     cudaStream_t s) {
+  return a.wide ? launch_tma_variant<L, SK, COLL, PITCH, true>(map, a, fullbc, rows, box, err, s)
+                : launch_tma_variant<L, SK, COLL, PITCH, false>(map, a, fullbc, rows, box, err, s);
 }
 
 template <int LAT, int SK, int COLL>
@@ -277,10 +293,18 @@ int launch_tma_t(const CUtensorMap& map, const StepArgs& a, bool fullbc, int row
   return launch_tma_pitch<L, SK, COLL, 1024>(map, a, fullbc, rows, box, err, s);
 }
 
-bool tma_x2_enabled();
+// Per-lattice entry points (step_tma_*.cu): raw FP16 with XLB-order BGK (code 0),
+// shifted FP16 / BF16 with BGK on the stored deviations (code 3); other
+// combinations return -1.
+template <int LAT>
+int launch_tma_lattice(const CUtensorMap& map, const StepArgs& a, int sk, int coll, bool fullbc, int rows, int box,
+                       int* err, cudaStream_t s) {
+  if (sk == SK_F16 && coll == 0) return launch_tma_t<LAT, SK_F16, 0>(map, a, fullbc, rows, box, err, s);
+  if (sk == SK_F16S && coll == 3) return launch_tma_t<LAT, SK_F16S, 3>(map, a, fullbc, rows, box, err, s);
+  if (sk == SK_BF16S && coll == 3) return launch_tma_t<LAT, SK_BF16S, 3>(map, a, fullbc, rows, box, err, s);
+  return -1;
+}
 
-// Per-lattice entry points (step_tma_*.cu).  sk: SK_F16 (XLB-order BGK) or
-// SK_F16S / SK_BF16S (pair-form BGK); other combinations return -1.
 int launch_step_tma_d2q9(const CUtensorMap& map, const StepArgs& a, int sk, int coll, bool fullbc, int rows,
                          int box, int* err, cudaStream_t s);
 int launch_step_tma_d3q19(const CUtensorMap& map, const StepArgs& a, int sk, int coll, bool fullbc, int rows,

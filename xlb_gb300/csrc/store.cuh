@@ -55,6 +55,12 @@ struct Store<SK_F16, T> {
 // by a power of two is exact, so each direction is one fused multiply-add whose
 // result equals the separately rounded form (f - w_l) * 2^14 and h * 2^-14 + w_l
 // bit for bit: fma(v, 2^14, -w 2^14) = RN(2^14 (v - w)) = 2^14 RN(v - w).
+//
+// The shifted forms also expose the stored deviation itself, g = kScale (f - w),
+// for the collision evaluated on deviations (collision code 3): dev / enc_dev
+// convert between the stored bits and g (one conversion each way), to_dev /
+// from_dev between g and f (one fused multiply-add each way; dec(b, w) ==
+// from_dev(dev(b), w) and enc(v, w) == enc_dev(to_dev(v, w)) bit for bit).
 template <>
 struct Store<SK_F16S, float> {
   using S = __half;
@@ -69,6 +75,10 @@ struct Store<SK_F16S, float> {
     return __half_as_ushort(__float2half_rn(__fmaf_rn(v, kScale, -(w * kScale))));
   }
   __device__ static __forceinline__ float dec_raw(Bits b) { return __half2float(__ushort_as_half(b)); }
+  __device__ static __forceinline__ float dev(Bits b) { return __half2float(__ushort_as_half(b)); }
+  __device__ static __forceinline__ Bits enc_dev(float g) { return __half_as_ushort(__float2half_rn(g)); }
+  __device__ static __forceinline__ float to_dev(float v, float w) { return __fmaf_rn(v, kScale, -(w * kScale)); }
+  __device__ static __forceinline__ float from_dev(float g, float w) { return __fmaf_rn(g, kInvScale, w); }
 };
 
 template <>
@@ -76,6 +86,8 @@ struct Store<SK_BF16S, float> {
   using S = __nv_bfloat16;
   using Bits = unsigned short;
   static constexpr bool shifted = true;
+  static constexpr float kScale = 1.0f;
+  static constexpr float kInvScale = 1.0f;
   __device__ static __forceinline__ float dec(Bits b, float w) {
     return __bfloat162float(__ushort_as_bfloat16(b)) + w;
   }
@@ -83,7 +95,30 @@ struct Store<SK_BF16S, float> {
     return __bfloat16_as_ushort(__float2bfloat16_rn(v - w));
   }
   __device__ static __forceinline__ float dec_raw(Bits b) { return __bfloat162float(__ushort_as_bfloat16(b)); }
+  __device__ static __forceinline__ float dev(Bits b) { return __bfloat162float(__ushort_as_bfloat16(b)); }
+  __device__ static __forceinline__ Bits enc_dev(float g) { return __bfloat16_as_ushort(__float2bfloat16_rn(g)); }
+  __device__ static __forceinline__ float to_dev(float v, float w) { return v - w; }
+  __device__ static __forceinline__ float from_dev(float g, float w) { return g + w; }
 };
+
+// A pulled population as the collision code works on it: f for codes 0-2, the
+// stored deviation g for code 3.
+template <int SK, class T, int COLL>
+__device__ __forceinline__ T load_pop(typename Store<SK, T>::Bits b, T w) {
+  if constexpr (COLL == 3)
+    return Store<SK, T>::dev(b);
+  else
+    return Store<SK, T>::dec(b, w);
+}
+
+// The stored bits of a post-collision population (f for codes 0-2, g for code 3).
+template <int SK, class T, int COLL>
+__device__ __forceinline__ typename Store<SK, T>::Bits store_pop(T v, T w) {
+  if constexpr (COLL == 3)
+    return Store<SK, T>::enc_dev(v);
+  else
+    return Store<SK, T>::enc(v, w);
+}
 
 template <class Bits>
 __device__ __forceinline__ Bits ldg_bits(const Bits* p) {

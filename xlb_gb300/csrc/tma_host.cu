@@ -3,27 +3,14 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
-#include <stdlib.h>
 
 #include <mutex>
 
 #include "../../include/xlbg.h"
+#include "ctx.cuh"
 #include "step_tma.cuh"
 
 namespace xlbg {
-
-// XLBG_TMA_X2=1 runs pair-form BGK with shifted 16-bit stores on the two-cell
-// consumer kernel (step_tma_x2.cuh; same results).  Off by default: at 512^3
-// D3Q19 it ran at 55.5 / 56.3 GLUPS (FP16S / BF16S) against the one-cell
-// kernel's 58.3 / 58.4 -- half the consumer warps per SM hide less latency
-// than the packed arithmetic saves.
-bool tma_x2_enabled() {
-  static const bool on = [] {
-    const char* e = getenv("XLBG_TMA_X2");
-    return e != nullptr && atoi(e) != 0;
-  }();
-  return on;
-}
 
 int fail(int code, const char* fmt, ...);
 
@@ -48,25 +35,22 @@ EncodeTiledFn encode_fn() {
   return fn;
 }
 
-bool tma_enabled() {
-  static const bool on = [] {
-    const char* e = getenv("XLBG_TMA");
-    return e == nullptr || atoi(e) != 0;
-  }();
-  return on;
-}
-
 std::mutex g_mu;
 int* g_fault_ptr[64] = {nullptr};
+void* g_fault_ctx[64] = {nullptr};
 
+// Device address of g_tma_fault on the current device, looked up again when the
+// device's context has changed (after cudaDeviceReset).
 int* fault_ptr() {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_fault_ptr[dev]) {
+  void* ctx = current_context();
+  if (!g_fault_ptr[dev] || ctx == nullptr || ctx != g_fault_ctx[dev]) {
     void* p = nullptr;
     if (cudaGetSymbolAddress(&p, g_tma_fault) != cudaSuccess) return nullptr;
     g_fault_ptr[dev] = static_cast<int*>(p);
+    g_fault_ctx[dev] = current_context();
   }
   return g_fault_ptr[dev];
 }
@@ -74,19 +58,22 @@ int* fault_ptr() {
 }  // namespace
 
 // Launches the TMA-staged step when it applies: a 16-bit store with FP32
-// compute (raw FP16 with BGK, FP16/BF16 shifted with pair-form BGK), no
-// diagnostics, a contiguous axis of 8..992 cells that is a multiple of 8, all
-// offsets within 32 bits and a 16-byte aligned f0.  Returns 1 when it does not
-// apply (the caller uses the marching kernel), else the status.
+// compute (raw FP16 with XLB-order BGK, FP16/BF16 shifted with BGK on the
+// stored deviations), no diagnostics, a contiguous axis of 8..992 cells that is
+// a multiple of 8, fewer than 2^31 cells and a 16-byte aligned f0.  Boundary
+// paths index planes in 32 bits when Q * cells < 2^32, else in 64 bits (as do
+// the calls made with a.wide set).  Returns 1 when it does not apply (the caller
+// uses the marching kernel), else the status.
 int try_launch_tma(const xlbg_desc* d, const StepArgs& a, bool fullbc, bool diag, cudaStream_t s) {
-  if (diag || !tma_enabled() || d->compute != XLBG_COMPUTE_F32) return 1;
+  if (diag || d->compute != XLBG_COMPUTE_F32) return 1;
   const int sk = d->store;
   const int coll = d->collision;
-  const bool combo = (sk == SK_F16 && coll == XLBG_BGK) || ((sk == SK_F16S || sk == SK_BF16S) && coll == XLBG_BGK_PAIR);
+  const bool combo =
+      (sk == SK_F16 && coll == XLBG_BGK) || ((sk == SK_F16S || sk == SK_BF16S) && coll == XLBG_BGK_SHIFTED);
   if (!combo) return 1;
   const int q = d->lattice == XLBG_D2Q9 ? 9 : (d->lattice == XLBG_D3Q19 ? 19 : 27);
   if (a.n2 < 8 || a.n2 > 992 || a.n2 % 8 != 0) return 1;
-  if ((long long)q * a.ncell > 0xffffffffLL) return 1;
+  if (a.ncell >= 0x7fffffffLL) return 1;
   if (reinterpret_cast<uintptr_t>(a.f0) % 16 != 0) return 1;
   EncodeTiledFn enc = encode_fn();
   int* err = fault_ptr();

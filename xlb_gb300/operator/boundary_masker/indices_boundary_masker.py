@@ -55,4 +55,5 @@ class IndicesBoundaryMasker(Operator):
                         _lib.ptr(bc_mask), _lib.ptr(missing_mask.view(torch.uint8)), _lib.stream_handle(),
                     )
                 )
+            _lib.mark_written(bc_mask, missing_mask)
         return bc_mask, missing_mask

@@ -153,4 +153,5 @@ class MeshBoundaryMasker(Operator):
                     _lib.stream_handle(),
                 )
             )
+        _lib.mark_written(bc_mask, missing_mask)
         return bc_mask, missing_mask

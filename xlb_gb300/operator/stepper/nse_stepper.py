@@ -16,9 +16,11 @@ cells, writes the BC aux values back into f_0.
 
 ``missing_mask`` keeps XLB's bool (q, nx, ny, nz) form.  The kernel reads a
 packed uint32 per cell instead; the packing happens once and is cached against
-the mask tensor (its storage and version counter), so modifying the mask in
-place triggers a repack.
+the mask tensor (the tensor object and its version counter), so modifying the
+mask in place -- by torch ops or by the maskers -- triggers a repack.
 """
+
+import weakref
 
 import numpy as np
 import torch
@@ -56,9 +58,13 @@ class IncompressibleNavierStokesStepper(Stepper):
     ):
         super().__init__(grid, boundary_conditions)
         if collision_type == "BGK":
-            # The shifted FP16/BF16 forms have no XLB counterpart and use BGK in pair
-            # form (same equations, fewer operations); the others keep XLB's order.
-            self.collision_code = _lib.BGK_PAIR if self.precision_policy.shifted else _lib.BGK
+            # The shifted FP16/BF16 forms have no XLB counterpart and run BGK on the
+            # stored deviations (same equations, pair form); the others keep XLB's order.
+            self.collision_code = _lib.BGK_SHIFTED if self.precision_policy.shifted else _lib.BGK
+        elif collision_type == "BGK_SHIFTED":
+            if not self.precision_policy.shifted:
+                raise ValueError("BGK_SHIFTED needs a shifted store (FP32FP16S or FP32BF16S)")
+            self.collision_code = _lib.BGK_SHIFTED
         elif collision_type == "BGK_PAIR":
             self.collision_code = _lib.BGK_PAIR
         elif collision_type == "KBC":
@@ -66,7 +72,7 @@ class IncompressibleNavierStokesStepper(Stepper):
                 raise NotImplementedError(f"Velocity set not supported for KBC: {self.velocity_set}")
             self.collision_code = _lib.KBC
         else:
-            raise NotImplementedError(f"collision_type {collision_type!r} is not on this path (BGK, BGK_PAIR, KBC)")
+            raise NotImplementedError(f"collision_type {collision_type!r} is not on this path (BGK, BGK_PAIR, BGK_SHIFTED, KBC)")
         if force_vector is not None:
             raise NotImplementedError("forced collision is not on this path")
         if streaming_scheme != "pull":
@@ -157,9 +163,20 @@ class IncompressibleNavierStokesStepper(Stepper):
                 raise ValueError(f"{name} must be contiguous")
 
     def _aux_state(self, bc_mask, missing_mask):
-        """(miss_bits, rec_cells, rec_scratch), cached against the two masks."""
-        key = (missing_mask.data_ptr(), missing_mask._version, bc_mask.data_ptr(), bc_mask._version)
-        if key == self._cache_key:
+        """(miss_bits, rec_cells, rec_scratch), cached against the two masks.
+
+        The cache holds weak references to the two mask tensors and their
+        version counters: another tensor object (even one reusing a freed
+        mask's memory) or an in-place change (torch ops bump the counter; the
+        maskers bump it after their C-ABI writes) triggers a repack."""
+        key = self._cache_key
+        if (
+            key is not None
+            and key[0]() is missing_mask
+            and key[1] == missing_mask._version
+            and key[2]() is bc_mask
+            and key[3] == bc_mask._version
+        ):
             return self._cache
         n = self.grid.num_cells
         bits = torch.empty(n, dtype=torch.int32, device=bc_mask.device)
@@ -169,7 +186,7 @@ class IncompressibleNavierStokesStepper(Stepper):
             ids = torch.tensor(self._rec_ids, dtype=torch.uint8, device=bc_mask.device)
             rec_cells = torch.nonzero(torch.isin(bc_mask.view(-1), ids)).view(-1).to(torch.int64).contiguous()
             scratch = torch.empty(max(1, rec_cells.numel()) * self.velocity_set.q, dtype=self.store_dtype, device=bc_mask.device)
-        self._cache_key = key
+        self._cache_key = (weakref.ref(missing_mask), missing_mask._version, weakref.ref(bc_mask), bc_mask._version)
         self._cache = (bits, rec_cells, scratch)
         return self._cache
 
