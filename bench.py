@@ -8,11 +8,14 @@ XLB's examples/performance/mlups_3d.py:87-90 counts them).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-Prints one JSON line.  The population fields (2 x 10.7 GB) are far larger than
-L2, so no L2 flush is needed between steps.  Under torchrun with N > 1 every
-rank runs the same workload on its own GPU (independent replicas, the path has
-no cross-GPU step here) and the value is the sum over ranks measured against
-the slowest rank.
+Prints one JSON line.  The population fields (2 x 10.2 GB) are far larger than
+L2, so no L2 flush is needed between steps.  Under torchrun with N > 1 the
+cavity is sharded along x as XLB shards it (xlb/distribute/distribute.py):
+weak scaling, a (512 N) x 512 x 512 cavity with one 512^3 slab per rank, the
+x-crossing populations of the slab faces exchanged every step over NCCL
+(point-to-point), timed against the slowest rank.  At N = 1 the line also
+carries the same cavity run as two slabs on the one GPU (device-local ghost
+exchange), the overhead of the sharded step.
 """
 
 import argparse
@@ -42,6 +45,7 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint/forward measurement")
+    p.add_argument("--no-slabs", action="store_true", help="skip the two-slab single-GPU measurement")
     return p.parse_args()
 
 
@@ -111,23 +115,8 @@ class ClockSampler:
 def cavity_setup(n, policy_name, omega=1.8):
     """The cavity: stepper and prepared fields on the current device; n is the
     cube edge or an (nx, ny, nz) shape."""
-    import numpy as np
-
-    import xlb_gb300 as xlb
-    from xlb_gb300.operator.boundary_condition import EquilibriumBC, FullwayBounceBackBC
-    from xlb_gb300.operator.stepper import IncompressibleNavierStokesStepper
-
-    pp = getattr(xlb.PrecisionPolicy, policy_name)
-    xlb.init(xlb.velocity_set.D3Q19(pp), xlb.ComputeBackend.CUDA, pp)
-    grid = xlb.grid.grid_factory((n, n, n) if isinstance(n, int) else tuple(n))
-    box = grid.bounding_box_indices()
-    nob = grid.bounding_box_indices(remove_edges=True)
-    walls = [box["bottom"][i] + box["left"][i] + box["right"][i] + box["front"][i] + box["back"][i] for i in range(3)]
-    walls = np.unique(np.array(walls), axis=-1).tolist()
-    bcs = [EquilibriumBC(rho=1.0, u=(0.05, 0.0, 0.0), indices=nob["top"]), FullwayBounceBackBC(indices=walls)]
-    stepper = IncompressibleNavierStokesStepper(grid, bcs, collision_type="BGK")
-    fields = stepper.prepare_fields()
-    return stepper, fields, omega
+    stepper = cavity_stepper((n, n, n) if isinstance(n, int) else tuple(n), policy_name)
+    return stepper, stepper.prepare_fields(), omega
 
 
 def timed_device(stepper, fields, omega, steps, warmup):
@@ -247,6 +236,114 @@ def cpu_baseline_sample(n=256, budget_s=10.0):
     }
 
 
+def cavity_stepper(shape, policy_name):
+    """The cavity stepper on a grid of ``shape`` without allocating its fields."""
+    import numpy as np
+
+    import xlb_gb300 as xlb
+    from xlb_gb300.operator.boundary_condition import EquilibriumBC, FullwayBounceBackBC
+    from xlb_gb300.operator.stepper import IncompressibleNavierStokesStepper
+
+    pp = getattr(xlb.PrecisionPolicy, policy_name)
+    xlb.init(xlb.velocity_set.D3Q19(pp), xlb.ComputeBackend.CUDA, pp)
+    grid = xlb.grid.grid_factory(tuple(shape))
+    box = grid.bounding_box_indices()
+    nob = grid.bounding_box_indices(remove_edges=True)
+    walls = [box["bottom"][i] + box["left"][i] + box["right"][i] + box["front"][i] + box["back"][i] for i in range(3)]
+    walls = np.unique(np.array(walls), axis=-1).tolist()
+    bcs = [EquilibriumBC(rho=1.0, u=(0.05, 0.0, 0.0), indices=nob["top"]), FullwayBounceBackBC(indices=walls)]
+    return IncompressibleNavierStokesStepper(grid, bcs, collision_type="BGK")
+
+
+def timed_slabs(ds, slabs, omega, steps, warmup):
+    """W untimed sharded steps, then K timed ones (exchange + step per slab),
+    bracketed by barrier + synchronize + CUDA events on the launching stream."""
+    import torch
+
+    ds.run(slabs, omega, warmup)
+    torch.cuda.synchronize()
+    barrier()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record()
+    ds.run(slabs, omega, steps, timestep0=warmup)
+    end.record()
+    torch.cuda.synchronize()
+    return start.elapsed_time(end)
+
+
+def slabs_on_one_gpu(n, steps, warmup, n_slabs=2):
+    """The n^3 cavity as n_slabs slabs on this GPU: MLUPS of the sharded step."""
+    from xlb_gb300.distribute import DistributedStepper, LocalTransport
+
+    st = cavity_stepper((n, n, n), "FP32FP32")
+    ds = DistributedStepper(st, n_slabs=n_slabs, transport=LocalTransport())
+    slabs = ds.prepare_fields()
+    ms = timed_slabs(ds, slabs, 1.8, steps, warmup)
+    return {"n_slabs": n_slabs, "MLUPS": n**3 * steps / (ms * 1e-3) / 1e6, "ms_per_step": ms / steps,
+            "what": f"{n}^3 FP32 cavity as {n_slabs} x-slabs on one GPU, ghost planes exchanged by device copies"}
+
+
+def run_sharded(args, world, rank, local):
+    """torchrun with N > 1: one 512^3 slab per rank of a (512 N) x 512 x 512
+    cavity, NCCL point-to-point ghost exchange every step (weak scaling)."""
+    import torch
+
+    from xlb_gb300.distribute import DistributedStepper, ProcessGroupTransport
+
+    n = args.n
+    st = cavity_stepper((n * world, n, n), "FP32FP32")
+    ds = DistributedStepper(st, transport=ProcessGroupTransport())
+    slabs = ds.prepare_fields()
+    cells = n**3  # per rank
+    peak, peak_kind = measured_peaks()
+    with ClockSampler(local) as clk:
+        ms = timed_slabs(ds, slabs, 1.8, args.steps, args.warmup)
+    ms = max_over_ranks(ms)
+    mlups = world * cells * args.steps / (ms * 1e-3) / 1e6
+    achieved = BYTES_PER_CELL[("D3Q19", 4)] * cells / (ms * 1e-3 / args.steps) / 1e9
+    out = {
+        "metric": METRIC, "value": mlups, "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {
+            "workload": f"D3Q19 BGK lid-driven cavity {n * world}x{n}x{n}, FP32FP32, sharded along x into {world} "
+                        f"slabs of {n}^3 (XLB's x sharding), NCCL point-to-point ghost exchange every step",
+            "cells": cells * world,
+            "l2": "inputs (2 x %.1f GB populations per rank) larger than L2; no flush" % (cells * 19 * 4 / 1e9),
+            "parallelism": f"slabs x{world}",
+        },
+        "gpu_launches": args.steps,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": load_traffic(n), "bytes_per_cell": BYTES_PER_CELL[("D3Q19", 4)],
+                     "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})"},
+        "clocks": clk.summary(),
+    }
+    if not args.no_e2e:
+        # end to end per rank: its slab's populations and masks H2D, K steps, f_0 D2H
+        (s,) = slabs
+        h_in = s.f_0.cpu().pin_memory()
+        h_out = torch.empty_like(h_in).pin_memory()
+        hb = s.bc_mask.cpu().pin_memory()
+        hm = s.missing_mask.cpu().pin_memory()
+        torch.cuda.synchronize()
+        barrier()
+        t0 = time.perf_counter()
+        s.f_0.copy_(h_in, non_blocking=True)
+        s.f_1.copy_(s.f_0)
+        s.bc_mask.copy_(hb, non_blocking=True)
+        s.missing_mask.copy_(hm, non_blocking=True)
+        ds.run(slabs, 1.8, args.steps)
+        h_out.copy_(s.f_0, non_blocking=True)
+        torch.cuda.synchronize()
+        dt = max_over_ranks(time.perf_counter() - t0)
+        out["e2e"] = {"value": world * cells * args.steps / dt / 1e6, "unit": "MLUPS",
+                      "h2d_bytes_per_step": (h_in.numel() * h_in.element_size() + hb.numel() + hm.numel()) / args.steps,
+                      "d2h_bytes_per_step": h_out.numel() * h_out.element_size() / args.steps,
+                      "what": "per rank: slab populations and masks H2D from pinned host, K sharded steps, slab f_0 D2H"}
+    if rank == 0:
+        print(json.dumps(out))
+
+
 def run_reference(args):
     """--impl reference: XLB's own CPU path needs warp or jax, neither installable
     here, so the C restatement of that path runs on this host's cores instead,
@@ -293,6 +390,10 @@ def main():
     from xlb_gb300 import _lib
 
     _lib.load()
+    if world > 1:
+        run_sharded(args, world, rank, local)
+        _dist.destroy_process_group()
+        return
     n = args.n
     cells = n**3
     peak, peak_kind = measured_peaks()
@@ -322,7 +423,7 @@ def main():
             "workload": f"D3Q19 BGK lid-driven cavity {n}^3, FP32FP32, FullwayBB x5 faces + EquilibriumBC lid u=(0.05,0,0), omega=1.8",
             "cells": cells,
             "l2": "inputs (2 x %.1f GB populations) larger than L2; no flush" % (cells * 19 * 4 / 1e9),
-            "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+            "parallelism": "single GPU",
         },
         "gpu_launches": args.steps,
         "roofline": {
@@ -351,6 +452,13 @@ def main():
             del st, fl
             torch.cuda.empty_cache()
         out["store_forms"] = forms
+        stepper, fields, omega = cavity_setup(n, "FP32FP32")
+    if not args.no_slabs:
+        del fields, stepper
+        torch.cuda.empty_cache()
+        out["slabs_one_gpu"] = slabs_on_one_gpu(n, args.steps, args.warmup)
+        out["slabs_one_gpu"]["x_single_domain"] = out["slabs_one_gpu"]["MLUPS"] / mlups
+        torch.cuda.empty_cache()
         stepper, fields, omega = cavity_setup(n, "FP32FP32")
     if not args.no_e2e:
         dt, h2d, d2h = timed_e2e(stepper, fields, omega, args.steps)

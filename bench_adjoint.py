@@ -30,7 +30,7 @@ import numpy as np
 import torch
 
 
-def _build(dim, policy_name, steps):
+def _build(dim, policy_name, steps, collision="BGK"):
     import xlb_gb300 as xlb
     from xlb_gb300.operator import boundary_condition as B
     from xlb_gb300.operator.boundary_condition import boundary_condition_registry as reg
@@ -63,7 +63,7 @@ def _build(dim, policy_name, steps):
         B.ZouHeBC("pressure", prescribed_value=1.0, indices=nob["right"]),
         B.HalfwayBounceBackBC(indices=obst),
     ]
-    stepper = IncompressibleNavierStokesStepper(grid, bcs, collision_type="BGK")
+    stepper = IncompressibleNavierStokesStepper(grid, bcs, collision_type=collision)
     f_0, f_1, bc_mask, missing = stepper.prepare_fields()
     run = stepper.differentiable(bc_mask, missing, 1.6, steps, checkpoint_every=100)
     # prescribed values as prepare_fields stored them (outlet density 1 stays);

@@ -54,9 +54,11 @@ enum { XLBG_COMPUTE_F32 = 0, XLBG_COMPUTE_F64 = 1 };
    with macroscopic and equilibrium rearranged over opposite-direction pairs (one
    reciprocal for u, shared pair terms): the same equations with fewer operations,
    results equal to XLBG_BGK up to rounding.  XLBG_BGK_SHIFTED is the pair form
-   evaluated on the stored deviations g = S (f - w_l) of the shifted stores
-   (XLBG_STORE_F16S / XLBG_STORE_BF16S only): one conversion per pulled and per
-   stored value, no FP32 rounding of f itself.  No XLB counterpart for 2 and 3. */
+   evaluated on deviations from rest, g = S (f - w_l): the stored values of the
+   shifted stores (XLBG_STORE_F16S / XLBG_STORE_BF16S; one conversion per pulled
+   and per stored value), or f - w_l for XLBG_STORE_F32 (exact on load, one
+   rounding on store), all with FP32 compute.  Sums of deviations do not cancel
+   the way sums of f ~ w_l do.  No XLB counterpart for 2 and 3. */
 enum { XLBG_BGK = 0, XLBG_KBC = 1, XLBG_BGK_PAIR = 2, XLBG_BGK_SHIFTED = 3 };
 
 /* boundary-condition kinds (xlb/operator/boundary_condition/bc_*.py) */

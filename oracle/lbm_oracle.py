@@ -159,19 +159,24 @@ class Store:
             return _bf16_to_f32(np.asarray(s)).astype(T)
         return np.asarray(s).astype(T)
 
-    # The shifted forms as the deviation-space collision (code 3) sees them:
-    # g = scale * (f - w_l) is the stored value itself.
+    # The populations as the deviation-space collision (code 3) sees them:
+    # g = scale * (f - w_l), the stored value itself for the shifted forms.
     @property
     def scale(self):
         return F16S_SCALE if self.kind == "f16s" else np.float32(1.0)
 
     def deviation(self, s):
-        """stored array -> float32 g (exact)."""
+        """stored array -> float32 g: the stored value of the shifted forms
+        (exact), f - w_l for FP32 (exact while w_l/2 <= f <= 2 w_l)."""
+        if self.kind == "f32":
+            return s.astype(np.float32) - self._w(np.float32, s.ndim)
         return s.astype(np.float32) if self.kind == "f16s" else _bf16_to_f32(s)
 
     def encode_deviation(self, g):
-        """float32 g -> stored array (round to nearest even)."""
+        """float32 g -> stored array (round to nearest even; FP32 stores w_l + g)."""
         g = np.asarray(g, dtype=np.float32)
+        if self.kind == "f32":
+            return (g + self._w(np.float32, g.ndim)).astype(np.float32)
         return g.astype(np.float16) if self.kind == "f16s" else _bf16_round(g)
 
     def to_deviation(self, f):
@@ -434,7 +439,8 @@ def bgk_shifted(lat, g, omega_t, scale):
     equilibrium + bgk (bgk.py:30-34, quadratic_equilibrium.py:35-60) in pair
     form, rewritten for g:
       rho = 1 + G/scale, v = 3u = 3 J/(scale rho), base = 1 - |v|^2/6,
-      per weight class k: A = omega scale w_k, C = A rho base - A,
+      r = rho base - 1 = (G/scale) base - |v|^2/6 (no cancellation),
+      per weight class k: A = omega scale w_k, C = A r,
       per pair (l, o) with t = c_l.v: R = C + (A rho / 2) t^2,
       g_out_l = (1 - omega) g_l + (A rho t + R), g_out_o = (1 - omega) g_o + (-A rho t + R).
     FP32 only; the operation order (and every fused multiply-add, fma32) is the
@@ -462,7 +468,9 @@ def bgk_shifted(lat, g, omega_t, scale):
     vsq = v[0] * v[0]
     for d in range(1, lat.d):
         vsq = fma32(v[d], v[d], vsq)
-    base = fma32(f32(-1.0) / f32(6.0), vsq, f32(1.0))
+    bm1 = (f32(-1.0) / f32(6.0)) * vsq
+    base = f32(1.0) + bm1
+    r = fma32(K * G, base, bm1)  # rho base - 1 without cancellation
     omf = f32(1.0) - f32(omega_t)
     norm1 = np.abs(lat.c).sum(axis=0)
     Ar, Arh, C = {}, {}, {}
@@ -471,7 +479,7 @@ def bgk_shifted(lat, g, omega_t, scale):
         A = f32(omega_t) * (S * wk)
         Ar[k] = A * rho
         Arh[k] = f32(0.5) * Ar[k]
-        C[k] = fma32(Ar[k], base, -A)
+        C[k] = A * r
     go = np.empty_like(g)
     go[0] = fma32(omf, g[0], C[0])
     for l in pairs:
@@ -734,13 +742,13 @@ def step(lat, store, f0, f1, bc_mask, missing, omega, bcs, collision="BGK", T=np
 
 
 def _step_shifted(lat, store, f0, f1, bc_mask, missing, omega, bcs, recovery):
-    """step() with collision code 3 (shifted stores, FP32): every pulled value,
+    """step() with collision code 3 (shifted or FP32 stores, FP32): every pulled value,
     streaming-step result and collision output is a stored deviation g.  The
     bounce-back kinds copy deviations (w_l = w_opp(l)), the extrapolation blend
     is the same linear expression on g, and EquilibriumBC / ZouHe / Regularized
     run on f between one from_deviation and one to_deviation per direction."""
-    if not store.shifted:
-        raise ValueError("BGK_SHIFTED needs a shifted store")
+    if not (store.shifted or store.kind == "f32"):
+        raise ValueError("BGK_SHIFTED needs a shifted or FP32 store")
     T = np.float32
     shp = f0.shape[1:]
     ids = bc_mask[0]

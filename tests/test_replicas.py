@@ -1,6 +1,6 @@
-"""The N-rank path of bench.py: independent replicas, a barrier around the timed
-region and the slowest rank's time (max over ranks), exercised with two gloo
-ranks on the CPU."""
+"""The N-rank timing of bench.py: a barrier around the timed region and the
+slowest rank's time (max over ranks), exercised with two gloo ranks on the CPU
+(the sharded step itself is covered by tests/test_slabs.py)."""
 
 import os
 import socket

@@ -187,3 +187,23 @@ def test_slab_diagnostics_match_single_domain(lattice, shape, layout, force_idx)
         assert np.allclose(got.cpu().numpy(), want.cpu().numpy(), rtol=1e-12, atol=1e-12)
     g0, _ = ds.gather(slabs)
     assert torch.equal(g0, f_0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("lattice,shape,layout", [("D3Q19", (16, 10, 10), "channel_regularized"),
+                                                  ("D3Q19", (15, 8, 8), "cavity_fullway"),
+                                                  ("D2Q9", (30, 18), "channel_zouhe")])
+def test_slab_prepare_fields_equals_scattered_global(lattice, shape, layout):
+    """prepare_fields() per slab (global masks, slab populations and aux values
+    only) gives the slabs that scattering the global prepare_fields() gives."""
+    from xlb_gb300.distribute import DistributedStepper, LocalTransport
+
+    sc = Scenario(lattice, shape, layout, policy="fp32")
+    ds = DistributedStepper(sc.stepper, n_slabs=3, transport=LocalTransport())
+    a = ds.scatter(*sc.stepper.prepare_fields())
+    for bc in sc.xbcs:
+        bc.is_initialized_with_aux_data = False
+    b = ds.prepare_fields()
+    for sa, sb in zip(a, b):
+        for name in ("f_0", "f_1", "bc_mask", "missing_mask"):
+            assert torch.equal(getattr(sa, name), getattr(sb, name)), (sa.index, name)

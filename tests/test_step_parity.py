@@ -234,3 +234,24 @@ def test_kernel_variants_match_oracle(lattice, shape, layout, policy, kernel):
     _compare(got0, want0, "f_0")
     _compare(got1, want1, "f_1")
     assert _lib.load().xlbg_device_faults(1) == 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("lattice,shape,layout", [
+    ("D2Q9", (30, 18), "channel_regularized"),
+    ("D2Q9", (24, 20), "cavity_fullway"),
+    ("D3Q19", (16, 10, 10), "channel_zouhe"),
+    ("D3Q19", (12, 10, 9), "cavity_halfway"),
+    ("D3Q19", (14, 9, 8), "channel_pressure"),
+    ("D3Q27", (16, 10, 10), "channel_regularized"),
+    ("D3Q19", (6, 5, 136), "cavity_fullway"),
+])
+def test_fp32_deviation_form_matches_oracle(lattice, shape, layout):
+    """collision_type="BGK_SHIFTED" with FP32 storage: BGK on g = f - w_l, bit
+    for bit against the oracle's restatement."""
+    sc = Scenario(lattice, shape, layout, policy="fp32", collision="BGK_SHIFTED")
+    sc.randomize(seed=15)
+    want0, want1 = sc.oracle_steps(4)
+    got0, got1 = sc.gpu_steps(4)
+    _compare(got0, want0, "f_0")
+    _compare(got1, want1, "f_1")

@@ -352,11 +352,7 @@ __device__ __forceinline__ void cell_adjoint(const AdjArgs& A, int i0, int i1, i
   T* __restrict__ lam_in = static_cast<T*>(A.lam_in);
   const long long N = a.ncell;
   int kind = 0;
-  if (id != 0) {
-#pragma unroll
-    for (int b = 0; b < kMaxBC; ++b)
-      if (b < a.nbc && a.bc[b].id == (int)id) kind = a.bc[b].kind;
-  }
+  if (id != 0) kind = (int)(a.bc_code[id] & 0xffu);
   if (kind == BC_EQUILIBRIUM) {  // f_post_stream = feq(rho_bc, u_bc): no dependence on f_t
 #pragma unroll
     for (int l = 0; l < Q; ++l) g[l] = T(0);

@@ -61,8 +61,10 @@ static int check_desc(const xlbg_desc* d) {
   if (d->collision != XLBG_BGK && d->collision != XLBG_KBC && d->collision != XLBG_BGK_PAIR &&
       d->collision != XLBG_BGK_SHIFTED)
     return fail(XLBG_ERR_ARG, "unknown collision %d", d->collision);
-  if (d->collision == XLBG_BGK_SHIFTED && d->store != XLBG_STORE_F16S && d->store != XLBG_STORE_BF16S)
-    return fail(XLBG_ERR_UNSUPPORTED, "BGK on stored deviations needs a shifted FP16/BF16 store");
+  if (d->collision == XLBG_BGK_SHIFTED &&
+      !(d->compute == XLBG_COMPUTE_F32 &&
+        (d->store == XLBG_STORE_F16S || d->store == XLBG_STORE_BF16S || d->store == XLBG_STORE_F32)))
+    return fail(XLBG_ERR_UNSUPPORTED, "BGK on deviations needs FP32 compute with an FP32 or shifted FP16/BF16 store");
   if (d->collision == XLBG_KBC && d->lattice == XLBG_D3Q19)
     return fail(XLBG_ERR_UNSUPPORTED, "KBC collision is defined for D2Q9 and D3Q27 only (kbc.py:184-185)");
   if (d->nx <= 0 || d->ny <= 0 || d->nz <= 0) return fail(XLBG_ERR_ARG, "grid shape must be positive");
@@ -300,6 +302,8 @@ int fill_step_args(const xlbg_desc* d, const void* f0, void* f1, const uint8_t* 
       a.bc[b].u[0] = a.bc[b].u[1] = a.bc[b].u[2] = 0.0;
     }
   }
+  for (int i = 0; i < 256; ++i) a.bc_code[i] = 0;
+  for (int b = 0; b < d->nbc; ++b) a.bc_code[d->bc[b].id & 0xff] = (uint16_t)(d->bc[b].kind | (b << 8));
   a.force_id = -1;
   a.diag_slots = nullptr;
   return XLBG_OK;

@@ -219,8 +219,8 @@ __device__ __forceinline__ void bgk_pair(const T (&f)[L::Q], T omega, T (&fo)[L:
   pair_update<L, T, 0>(f, u, base, omf, orho, fo);
 }
 
-// BGK on the stored deviations of the shifted FP16 / BF16 forms (collision
-// code 3; no XLB counterpart).  The same equations as macroscopic + quadratic
+// BGK on the stored deviations of the shifted FP16 / BF16 forms, and on
+// g = f - w for FP32 storage (collision code 3; no XLB counterpart).  The same equations as macroscopic + quadratic
 // equilibrium + BGK (bgk.py:30-34, quadratic_equilibrium.py:35-60), written
 // for g_l = S (f_l - w_l) as the store holds it (S = 2^14 for FP16S, 1 for
 // BF16S) so that a pulled value is one conversion from its bits and a result
@@ -230,15 +230,15 @@ __device__ __forceinline__ void bgk_pair(const T (&f)[L::Q], T omega, T (&fo)[L:
 //   S (feq_l - w_l) = S w_l (rho e_l - 1),  e_l = 1 + t + t^2 / 2 - 1.5 |u|^2,  t = 3 c_l.u,
 //   g_out = (1 - omega) g + omega S (feq - w).
 // Over an opposite pair (l, o) t changes sign; with A = omega S w (one per
-// weight class), v = 3u, base = 1 - |v|^2 / 6, C = A rho base - A (one fused
-// multiply-add per class) and R = C + (A rho / 2) t^2:
+// weight class), v = 3u, base = 1 - |v|^2 / 6, C = A (rho base - 1) and
+// R = C + (A rho / 2) t^2:
 //   g_out_l = fma(1 - omega, g_l, fma( A rho, t, R)),
 //   g_out_o = fma(1 - omega, g_o, fma(-A rho, t, R)).
 // About 125 floating-point operations per D3Q19 cell, decode and encode
 // included, against about 200 for the pair form on f.
 template <int SK>
 __host__ __device__ constexpr float shift_scale() {
-  return SK == 3 ? 16384.0f : 1.0f;  // SK_F16S : SK_BF16S
+  return SK == 3 ? 16384.0f : 1.0f;  // SK_F16S : SK_BF16S and SK_F32 (g = f - w)
 }
 
 template <class L, int P>
@@ -284,7 +284,11 @@ __device__ __forceinline__ void bgk_shifted(const float (&g)[L::Q], float omega,
   float vsq = v[0] * v[0];
 #pragma unroll
   for (int d = 1; d < L::D; ++d) vsq = __fmaf_rn(v[d], v[d], vsq);
-  const float base = __fmaf_rn(-1.0f / 6.0f, vsq, 1.0f);
+  // rho base - 1 = (1 + G/S)(1 + bm1) - 1 = (G/S) base + bm1, bm1 = -|v|^2/6: no
+  // cancellation against the 1 of rho or of base
+  const float bm1 = (-1.0f / 6.0f) * vsq;
+  const float base = 1.0f + bm1;
+  const float r = __fmaf_rn(K * G, base, bm1);
   const float omf = 1.0f - omega;
   float Ar[4] = {0.0f, 0.0f, 0.0f, 0.0f}, Arh[4] = {0.0f, 0.0f, 0.0f, 0.0f}, C[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll
@@ -293,7 +297,7 @@ __device__ __forceinline__ void bgk_shifted(const float (&g)[L::Q], float omega,
     const float A = omega * (S * (float)class_weight<L>(k));
     Ar[k] = A * rho;
     Arh[k] = 0.5f * Ar[k];
-    C[k] = __fmaf_rn(Ar[k], base, -A);
+    C[k] = A * r;
   }
   go[0] = __fmaf_rn(omf, g[0], C[0]);
   shifted_pair_update<L, 0>(g, v, Ar, Arh, C, omf, go);

@@ -24,9 +24,10 @@ int launch_step_t(const StepArgs& a, int sk, int compute, bool fullbc, bool diag
     else                                                                             \
       step_kernel<L, SKV, TV, COLL, false, false><<<grid, kStepBlock, 0, s>>>(a);   \
   } while (0)
-  if constexpr (COLL == 3) {  // stored deviations: shifted stores, FP32 compute only
+  if constexpr (COLL == 3) {  // deviations: shifted stores or FP32, FP32 compute only
     if (compute == 1) return -1;
     switch (sk) {
+      case SK_F32: XLBG_LAUNCH(SK_F32, float); break;
       case SK_F16S: XLBG_LAUNCH(SK_F16S, float); break;
       case SK_BF16S: XLBG_LAUNCH(SK_BF16S, float); break;
       default: return -1;
@@ -79,9 +80,10 @@ int launch_step_march_t(const StepArgs& a, int sk, int compute, bool fullbc, int
   const int zblocks = (a.n2 + threads - 1) / threads;
   const dim3 grid((unsigned)(a.n0 * zblocks), (unsigned)((a.n1 + chunk - 1) / chunk));
 #define XLBG_MLAUNCH(SKV, TV) launch_march_variant<L, SKV, TV, COLL>(a, fullbc, grid, threads, chunk, s)
-  if constexpr (COLL == 3) {  // stored deviations: shifted stores, FP32 compute only
+  if constexpr (COLL == 3) {  // deviations: shifted stores or FP32, FP32 compute only
     if (compute == 1) return -1;
     switch (sk) {
+      case SK_F32: XLBG_MLAUNCH(SK_F32, float); break;
       case SK_F16S: XLBG_MLAUNCH(SK_F16S, float); break;
       case SK_BF16S: XLBG_MLAUNCH(SK_BF16S, float); break;
       default: return -1;

@@ -54,6 +54,9 @@ struct StepArgs {
   float omega_f;  // omega rounded to float on the host (same RN conversion as in-kernel)
   double extrap_cs;
   BCEntry bc[kMaxBC];
+  // per bc_mask id: kind | (index into bc) << 8; 0 for ids without a BC.  One
+  // constant load per boundary cell instead of a scan over the BC list.
+  uint16_t bc_code[256];
   int force_id;
   double* diag_slots;  // kDiagSlots x 4 doubles, zero on entry
 };
@@ -197,21 +200,14 @@ __device__ __forceinline__ void cell_update(const StepArgs& a, int i0, int i1, i
   using Bits = typename St::Bits;
   constexpr int Q = L::Q;
   const int n1 = a.n1, n2 = a.n2;
-  // ---- boundary lookup (XLB unrolls the BC list the same way, nse_stepper.py:280-293) ----
+  // ---- boundary lookup (XLB unrolls the BC list, nse_stepper.py:280-293; here
+  // one table load gives the kind and the BC's slot) ----
   int kind = 0;
-  double bc_rho = 0.0, bc_u[3] = {0.0, 0.0, 0.0};
   uint32_t miss = 0;
   if (id != 0) {
-#pragma unroll
-    for (int b = 0; b < kMaxBC; ++b) {
-      if (b < a.nbc && a.bc[b].id == (int)id) {
-        kind = a.bc[b].kind;
-        bc_rho = a.bc[b].rho;
-        bc_u[0] = a.bc[b].u[0];
-        bc_u[1] = a.bc[b].u[1];
-        bc_u[2] = a.bc[b].u[2];
-      }
-    }
+    const unsigned code = a.bc_code[id];
+    kind = (int)(code & 0xffu);
+    const int slot = (int)(code >> 8);
     const bool need_miss = kind == BC_HALFWAY || kind == BC_EXTRAP || kind == BC_ZOUHE_V || kind == BC_ZOUHE_P ||
                            kind == BC_REG_V || kind == BC_REG_P || (DIAG && (int)id == a.force_id);
     if (need_miss) miss = __ldg(a.miss + cell);
@@ -228,8 +224,8 @@ __device__ __forceinline__ void cell_update(const StepArgs& a, int i0, int i1, i
       // bc_equilibrium.py:255-271
       T u[L::D];
 #pragma unroll
-      for (int d = 0; d < L::D; ++d) u[d] = T(bc_u[d]);
-      equilibrium<L>(T(bc_rho), u, f);
+      for (int d = 0; d < L::D; ++d) u[d] = T(a.bc[slot].u[d]);
+      equilibrium<L>(T(a.bc[slot].rho), u, f);
       if constexpr (COLL == 3) {
 #pragma unroll
         for (int l = 0; l < Q; ++l) f[l] = St::to_dev(f[l], T(weight<L>(l)));

@@ -25,6 +25,12 @@ struct Store<SK_F32, T> {
   __device__ static __forceinline__ T dec(Bits b, T) { return (T)__uint_as_float(b); }
   __device__ static __forceinline__ Bits enc(T v, T) { return __float_as_uint((float)v); }
   __device__ static __forceinline__ T dec_raw(Bits b) { return (T)__uint_as_float(b); }
+  // deviation form (collision code 3, FP32 compute): g = f - w_l, exact for
+  // w_l / 2 <= f <= 2 w_l (Sterbenz); the store rounds f = w_l + g once
+  __device__ static __forceinline__ T dev(Bits b, T w) { return __uint_as_float(b) - w; }
+  __device__ static __forceinline__ Bits enc_dev(T g, T w) { return __float_as_uint(g + w); }
+  __device__ static __forceinline__ T to_dev(T v, T w) { return v - w; }
+  __device__ static __forceinline__ T from_dev(T g, T w) { return g + w; }
 };
 
 template <class T>
@@ -58,9 +64,10 @@ struct Store<SK_F16, T> {
 //
 // The shifted forms also expose the stored deviation itself, g = kScale (f - w),
 // for the collision evaluated on deviations (collision code 3): dev / enc_dev
-// convert between the stored bits and g (one conversion each way), to_dev /
-// from_dev between g and f (one fused multiply-add each way; dec(b, w) ==
-// from_dev(dev(b), w) and enc(v, w) == enc_dev(to_dev(v, w)) bit for bit).
+// convert between the stored bits and g (one conversion each way; w unused),
+// to_dev / from_dev between g and f (one fused multiply-add each way;
+// dec(b, w) == from_dev(dev(b, w), w) and enc(v, w) == enc_dev(to_dev(v, w), w)
+// bit for bit).
 template <>
 struct Store<SK_F16S, float> {
   using S = __half;
@@ -75,8 +82,8 @@ struct Store<SK_F16S, float> {
     return __half_as_ushort(__float2half_rn(__fmaf_rn(v, kScale, -(w * kScale))));
   }
   __device__ static __forceinline__ float dec_raw(Bits b) { return __half2float(__ushort_as_half(b)); }
-  __device__ static __forceinline__ float dev(Bits b) { return __half2float(__ushort_as_half(b)); }
-  __device__ static __forceinline__ Bits enc_dev(float g) { return __half_as_ushort(__float2half_rn(g)); }
+  __device__ static __forceinline__ float dev(Bits b, float) { return __half2float(__ushort_as_half(b)); }
+  __device__ static __forceinline__ Bits enc_dev(float g, float) { return __half_as_ushort(__float2half_rn(g)); }
   __device__ static __forceinline__ float to_dev(float v, float w) { return __fmaf_rn(v, kScale, -(w * kScale)); }
   __device__ static __forceinline__ float from_dev(float g, float w) { return __fmaf_rn(g, kInvScale, w); }
 };
@@ -95,8 +102,10 @@ struct Store<SK_BF16S, float> {
     return __bfloat16_as_ushort(__float2bfloat16_rn(v - w));
   }
   __device__ static __forceinline__ float dec_raw(Bits b) { return __bfloat162float(__ushort_as_bfloat16(b)); }
-  __device__ static __forceinline__ float dev(Bits b) { return __bfloat162float(__ushort_as_bfloat16(b)); }
-  __device__ static __forceinline__ Bits enc_dev(float g) { return __bfloat16_as_ushort(__float2bfloat16_rn(g)); }
+  __device__ static __forceinline__ float dev(Bits b, float) { return __bfloat162float(__ushort_as_bfloat16(b)); }
+  __device__ static __forceinline__ Bits enc_dev(float g, float) {
+    return __bfloat16_as_ushort(__float2bfloat16_rn(g));
+  }
   __device__ static __forceinline__ float to_dev(float v, float w) { return v - w; }
   __device__ static __forceinline__ float from_dev(float g, float w) { return g + w; }
 };
@@ -106,7 +115,7 @@ struct Store<SK_BF16S, float> {
 template <int SK, class T, int COLL>
 __device__ __forceinline__ T load_pop(typename Store<SK, T>::Bits b, T w) {
   if constexpr (COLL == 3)
-    return Store<SK, T>::dev(b);
+    return Store<SK, T>::dev(b, w);
   else
     return Store<SK, T>::dec(b, w);
 }
@@ -115,7 +124,7 @@ __device__ __forceinline__ T load_pop(typename Store<SK, T>::Bits b, T w) {
 template <int SK, class T, int COLL>
 __device__ __forceinline__ typename Store<SK, T>::Bits store_pop(T v, T w) {
   if constexpr (COLL == 3)
-    return Store<SK, T>::enc_dev(v);
+    return Store<SK, T>::enc_dev(v, w);
   else
     return Store<SK, T>::enc(v, w);
 }

@@ -242,11 +242,47 @@ class DistributedStepper:
         return [self._slab_from_global(r, f_0, f_1, bc_mask, missing_mask, dev) for r in self.local]
 
     def prepare_fields(self, device=None):
-        """The local slabs of the stepper's prepare_fields(): the global fields
-        are built on ``device`` (default: the grid's), sliced, and released."""
-        f_0, f_1, bc_mask, missing_mask = self.stepper.prepare_fields()
-        slabs = self.scatter(f_0, f_1, bc_mask, missing_mask, device)
-        del f_0, f_1, bc_mask, missing_mask
+        """The local slabs of the stepper's prepare_fields() without global
+        populations: the masks are built for the whole grid (XLB's maskers need
+        the global bounds) on ``device`` (default: the current CUDA device),
+        sliced and released; each slab's f_0 is the rest equilibrium and its
+        f_1 a copy carrying the ZouHe / Regularized aux values of its cells
+        (boundary_condition.py:130-159, evaluated at global indices)."""
+        from xlb_gb300.helper.initializers import initialize_eq
+
+        st = self.stepper
+        vs = st.velocity_set
+        dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        fs = tuple(st.grid.field_shape)
+        bc_mask = torch.zeros((1,) + fs, dtype=torch.uint8, device=dev)
+        missing = torch.zeros((vs.q,) + fs, dtype=torch.bool, device=dev)
+        bc_mask, missing = st._process_boundary_conditions(st.boundary_conditions, bc_mask, missing)
+        cdt = st.precision_policy.compute_precision.torch_dtype
+        slabs = []
+        for r in self.local:
+            planes = torch.tensor(self.layout.padded_planes(r), dtype=torch.long, device=dev)
+            x0, x1 = self.layout.bounds[r]
+            bm = bc_mask.index_select(1, planes).contiguous()
+            bm[:, 0] = 255
+            bm[:, -1] = 255
+            mm = missing.index_select(1, planes).contiguous()
+            mm[:, 0] = False
+            mm[:, -1] = False
+            f_0 = torch.empty((vs.q,) + tuple(bm.shape[1:]), dtype=st.store_dtype, device=dev)
+            f_0 = initialize_eq(f_0, None, vs, st.precision_policy)
+            f_1 = f_0.clone()
+            for bc in st.boundary_conditions:
+                if not bc.needs_aux_init:
+                    continue
+                lin = torch.nonzero(bm.view(-1) == bc.id).view(-1)
+                if lin.numel() == 0:
+                    continue
+                idx = np.array(np.unravel_index(lin.cpu().numpy(), tuple(bm.shape[1:])))
+                idx[0] = (x0 - 1 + idx[0]) % self.layout.nx  # padded plane -> global x
+                vals = torch.as_tensor(bc.aux_values(idx), dtype=torch.float64, device=dev)
+                f_1[0].view(-1)[lin] = vals.to(cdt).to(f_1.dtype)
+            slabs.append(SlabFields(r, x0, x1, f_0, f_1, bm, mm))
+        del bc_mask, missing
         return slabs
 
     def gather(self, slabs):

@@ -62,8 +62,10 @@ class IncompressibleNavierStokesStepper(Stepper):
             # stored deviations (same equations, pair form); the others keep XLB's order.
             self.collision_code = _lib.BGK_SHIFTED if self.precision_policy.shifted else _lib.BGK
         elif collision_type == "BGK_SHIFTED":
-            if not self.precision_policy.shifted:
-                raise ValueError("BGK_SHIFTED needs a shifted store (FP32FP16S or FP32BF16S)")
+            pp = self.precision_policy
+            if not (pp.shifted or (pp.store_code, pp.compute_code) == (0, 0)):
+                raise ValueError("BGK_SHIFTED needs FP32 compute with a shifted or FP32 store "
+                                 "(FP32FP16S, FP32BF16S, FP32FP32)")
             self.collision_code = _lib.BGK_SHIFTED
         elif collision_type == "BGK_PAIR":
             self.collision_code = _lib.BGK_PAIR
