@@ -20,6 +20,8 @@ from _scenarios import Scenario
         ("D2Q9", (30, 18), "channel_zouhe", "BGK", 3),
         ("D3Q27", (16, 10, 10), "channel_regularized", "KBC", 3),
         ("D3Q19", (12, 10, 9), "cavity_halfway", "BGK", 1),
+        # FP32 D3Q27 KBC on a contiguous axis of 16: the TMA-staged diagnostics step
+        ("D3Q27", (16, 10, 16), "channel_regularized", "KBC", 3),
     ],
 )
 def test_diagnostics_match_oracle(lattice, shape, layout, collision, force_idx, policy):

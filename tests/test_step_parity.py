@@ -255,3 +255,32 @@ def test_fp32_deviation_form_matches_oracle(lattice, shape, layout):
     got0, got1 = sc.gpu_steps(4)
     _compare(got0, want0, "f_0")
     _compare(got1, want1, "f_1")
+
+
+KBC_TMA_CASES = [
+    # FP32 D3Q27 KBC with a contiguous axis of 8..512 cells (4-byte multiples of 16 bytes):
+    # the TMA-staged kernel, staged rows of 192, 256 and 512 cells
+    ("D3Q27", (10, 8, 16), "channel_regularized"),
+    ("D3Q27", (10, 8, 16), "channel_zouhe"),
+    ("D3Q27", (6, 5, 192), "periodic"),
+    ("D3Q27", (5, 4, 264), "cavity_halfway"),
+    ("D3Q27", (6, 5, 200), "channel_pressure"),
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kernel", ["auto", "tma_wide"])
+@pytest.mark.parametrize("lattice,shape,layout", KBC_TMA_CASES)
+def test_kbc_fp32_tma_matches_oracle(lattice, shape, layout, kernel):
+    from xlb_gb300 import _lib
+
+    sc = Scenario(lattice, shape, layout, policy="fp32", collision="KBC")
+    sc.randomize(seed=16)
+    if layout == "periodic":
+        sc.bc_mask[0, 1:3, 0:2, 100:140] = 255  # skip cells inside staged rows
+    want0, want1 = sc.oracle_steps(3)
+    with _lib.forced_kernel(_lib.KERNEL_AUTO if kernel == "auto" else _lib.KERNEL_TMA_WIDE):
+        got0, got1 = sc.gpu_steps(3)
+    _compare(got0, want0, "f_0")
+    _compare(got1, want1, "f_1")
+    assert _lib.load().xlbg_device_faults(1) == 0

@@ -291,10 +291,14 @@ __device__ __forceinline__ void bgk_shifted(const float (&g)[L::Q], float omega,
   const float r = __fmaf_rn(K * G, base, bm1);
   const float omf = 1.0f - omega;
   float Ar[4] = {0.0f, 0.0f, 0.0f, 0.0f}, Arh[4] = {0.0f, 0.0f, 0.0f, 0.0f}, C[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+  // the class weights as compile-time constants (class_weight called with the
+  // unrolled index below would not be a constant expression and ran as a loop)
+  constexpr float Sw[4] = {S * (float)class_weight<L>(0), S * (float)class_weight<L>(1),
+                           S * (float)class_weight<L>(2), S * (float)class_weight<L>(3)};
 #pragma unroll
   for (int k = 0; k <= L::D; ++k) {
     // weight class |c|_1 = k (D2Q9 and D3Q19 have no k = 3; the unused entries fold away)
-    const float A = omega * (S * (float)class_weight<L>(k));
+    const float A = omega * Sw[k];
     Ar[k] = A * rho;
     Arh[k] = 0.5f * Ar[k];
     C[k] = A * r;

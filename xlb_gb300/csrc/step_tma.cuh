@@ -110,32 +110,35 @@ __host__ __device__ constexpr int tma_consumers() {
   return PITCH > 992 ? 992 : PITCH;
 }
 
-// CTAs per SM the launch bounds ask for (consumers + one producer warp).
-template <int PITCH>
+// CTAs per SM the launch bounds ask for (consumers + one producer warp): 16-bit
+// BGK, whose cells need few registers, as many as the shared memory allows;
+// 4-byte stores (KBC) one: asking for two capped KBC at 96 registers with
+// spills, while its ~128 registers still fit two 224-thread CTAs (PITCH 192).
+template <int EB, int PITCH>
 __host__ __device__ constexpr int tma_min_blocks() {
-  return PITCH <= 256 ? 4 : (PITCH == 512 ? 2 : 1);
+  return EB == 2 ? (PITCH <= 256 ? 4 : (PITCH == 512 ? 2 : 1)) : 1;
 }
 
-// shared memory: S stages of Q rows, then S "full" and S "empty" mbarriers
-template <class L, int PITCH>
+// shared memory: S stages of Q rows of EB-byte elements, then S "full" and S "empty" mbarriers
+template <class L, int EB, int PITCH>
 __host__ __device__ constexpr unsigned tma_smem_bytes() {
-  return (unsigned)tma_stages<L>() * L::Q * PITCH * 2 + 16u * tma_stages<L>();
+  return (unsigned)tma_stages<L>() * L::Q * PITCH * EB + 16u * tma_stages<L>();
 }
 
 // Producer warp of a TMA-staged step CTA: lane l < Q issues the copies of
 // direction l, row after row, into the S-stage ring at base (see the hand-off
 // described at step_kernel_tma).  A bounded wait that runs out counts one
 // fault, lets the copies still in flight land and returns.
-template <class L, int PITCH>
+template <class L, int EB, int PITCH>
 __device__ __forceinline__ void tma_produce(const CUtensorMap& map, unsigned base, unsigned full, unsigned empty, int l,
                                             int i0, int r0, int nr, int n0, int n1, int n2, int box, int* err) {
   constexpr int Q = L::Q;
   constexpr int S = tma_stages<L>();
-  constexpr unsigned ROW = PITCH * 2;
+  constexpr unsigned ROW = PITCH * EB;
   constexpr unsigned STAGE = Q * ROW;
   const bool issuer = l < Q;
   const int nbox = (n2 + box - 1) / box;
-  const unsigned tx_bytes = (unsigned)(Q * nbox * box * 2);
+  const unsigned tx_bytes = (unsigned)(Q * nbox * box * EB);
   const int c0 = issuer ? axis_c<L>(l, 0) : 0, c1 = issuer ? axis_c<L>(l, 1) : 0;
   const int xs = c0 == 1 ? (i0 == 0 ? n0 - 1 : i0 - 1) : (c0 == -1 ? (i0 == n0 - 1 ? 0 : i0 + 1) : i0);
   for (int k = 0; k < nr; ++k) {
@@ -158,17 +161,21 @@ __device__ __forceinline__ void tma_produce(const CUtensorMap& map, unsigned bas
       const int y = r0 + k;
       const int ys = c1 == 1 ? (y == 0 ? n1 - 1 : y - 1) : (c1 == -1 ? (y == n1 - 1 ? 0 : y + 1) : y);
       for (int b = 0; b < nbox; ++b)
-        tma_load_4d(base + s * STAGE + (unsigned)l * ROW + b * box * 2, &map, b * box, ys, xs, l, bar);
+        tma_load_4d(base + s * STAGE + (unsigned)l * ROW + b * box * EB, &map, b * box, ys, xs, l, bar);
     }
   }
 }
 
-// map: 4D tensor map of f0 as (n2, n1, n0, Q) 16-bit elements, box (box, 1, 1, 1)
-// with box = min(n2, 256).  Grid: (n0, ceil(n1 / rows)); CT + 32 threads per
-// block, CT = tma_consumers<PITCH>(): CT consumers (thread i2 owns cell i2 of
-// every row) and one producer warp, whose lanes issue the copies.  Staged rows
-// hold PITCH elements; n2 <= CT, n2 % 8 == 0; cell offsets fit 31 bits (the host
-// checks).  Plane offsets: the fluid path stores through the cell's slot in
+// map: 4D tensor map of f0 as (n2, n1, n0, Q) elements of the store (2 or 4
+// bytes), box (box, 1, 1, 1) with box = min(n2, 256).  Grid: (n0, ceil(n1 /
+// rows)); CT + 32 threads per block, CT = tma_consumers<PITCH>(): CT consumers
+// (thread i2 owns cell i2 of every row) and one producer warp, whose lanes issue
+// the copies.  Staged rows hold PITCH elements; n2 <= CT, n2 * element bytes a
+// multiple of 16; cell offsets fit 31 bits (the host checks).  DIAG: the
+// diagnostics step (mass of the output, force on the input, as the marching
+// kernel's): per-thread FP64 sums, reduced over each consumer warp by shuffles
+// and added to the slot array by lane 0 (no block barrier: the producer warp
+// has left).  Plane offsets: the fluid path stores through the cell's slot in
 // plane 0 plus 64-bit plane offsets at any size; the boundary paths index
 // f0 / f1 planes with Idx, 32-bit unsigned when Q * cells < 2^32 and 64-bit
 // (WIDE) above, e.g. for 1024 x 1024 x 768 cells.
@@ -179,17 +186,19 @@ __device__ __forceinline__ void tma_produce(const CUtensorMap& map, unsigned bas
 //   consumer warp: wait full[s] phase u, read its cells, __syncwarp, lane 0
 //                  arrives on empty[s] (CT / 32 arrivals complete the phase)
 // No block-wide barrier after set-up: consumer warps drift up to S rows apart.
-template <class L, int SK, int COLL, bool FULLBC, int PITCH, bool WIDE>
-__global__ void __launch_bounds__(tma_consumers<PITCH>() + 32, tma_min_blocks<PITCH>())
+template <class L, int SK, int COLL, bool FULLBC, int PITCH, bool WIDE, bool DIAG = false>
+__global__ void __launch_bounds__(tma_consumers<PITCH>() + 32,
+                                  tma_min_blocks<sizeof(typename Store<SK, float>::Bits), PITCH>())
     step_kernel_tma(const __grid_constant__ CUtensorMap map, const StepArgs a, int rows, int box, int* err) {
   using T = float;
   using Idx = typename std::conditional<WIDE, long long, unsigned>::type;
   using St = Store<SK, T>;
   using Bits = typename St::Bits;
-  static_assert(sizeof(Bits) == 2, "16-bit stores only");
+  constexpr int EB = sizeof(Bits);
+  static_assert(EB == 2 || EB == 4, "16- or 32-bit stores");
   constexpr int Q = L::Q;
   constexpr int S = tma_stages<L>();
-  constexpr unsigned ROW = PITCH * 2;
+  constexpr unsigned ROW = PITCH * EB;
   constexpr unsigned STAGE = Q * ROW;
   constexpr int CT = tma_consumers<PITCH>();
   constexpr unsigned CONSUMER_WARPS = CT / 32;
@@ -216,7 +225,7 @@ __global__ void __launch_bounds__(tma_consumers<PITCH>() + 32, tma_min_blocks<PI
   __syncthreads();
 
   if (tid >= CT) {
-    tma_produce<L, PITCH>(map, base, full, empty, tid - CT, i0, r0, nr, n0, n1, n2, box, err);
+    tma_produce<L, EB, PITCH>(map, base, full, empty, tid - CT, i0, r0, nr, n0, n1, n2, box, err);
     return;
   }
 
@@ -225,8 +234,8 @@ __global__ void __launch_bounds__(tma_consumers<PITCH>() + 32, tma_min_blocks<PI
   const int i2 = tid;
   const bool active = i2 < n2;
   // byte offset in a staged row of the source element for c2 = -1, 0, +1
-  const unsigned zb[3] = {(unsigned)(i2 == n2 - 1 ? 0 : i2 + 1) * 2, (unsigned)i2 * 2,
-                          (unsigned)(i2 == 0 ? n2 - 1 : i2 - 1) * 2};
+  const unsigned zb[3] = {(unsigned)(i2 == n2 - 1 ? 0 : i2 + 1) * EB, (unsigned)i2 * EB,
+                          (unsigned)(i2 == 0 ? n2 - 1 : i2 - 1) * EB};
   double dm = 0.0, df[3] = {0.0, 0.0, 0.0};
   // the bc ids run one row ahead, so their load latency hides behind a row's collision
   const unsigned row0 = ((unsigned)i0 * (unsigned)n1 + (unsigned)r0) * (unsigned)n2 + (unsigned)i2;
@@ -252,45 +261,92 @@ __global__ void __launch_bounds__(tma_consumers<PITCH>() + 32, tma_min_blocks<PI
     }
     __syncwarp();
     if (lane == 0) mbar_arrive(empty + 8 * s);
-    if (id != 255) cell_update<L, SK, T, COLL, FULLBC, false>(a, i0, y, i2, (Idx)cell, id, f, dm, df);
+    if constexpr (DIAG) {
+      if (id != 255) {
+        double dmc = 0.0, dfc[3] = {0.0, 0.0, 0.0};
+        cell_update<L, SK, T, COLL, FULLBC, true>(a, i0, y, i2, (Idx)cell, id, f, dmc, dfc);
+        dm += dmc;
+        df[0] += dfc[0];
+        df[1] += dfc[1];
+        df[2] += dfc[2];
+      }
+    } else {
+      if (id != 255) cell_update<L, SK, T, COLL, FULLBC, false>(a, i0, y, i2, (Idx)cell, id, f, dm, df);
+    }
+  }
+  if constexpr (DIAG) {
+    double v[4] = {dm, df[0], df[1], df[2]};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+    }
+    if (lane == 0) {
+      const unsigned slot = ((blockIdx.x * gridDim.y + blockIdx.y) * CONSUMER_WARPS + (tid >> 5)) % kDiagSlots;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) atomicAdd(a.diag_slots + slot * 4 + k, v[k]);
+    }
   }
 }
 
 // Launch for one (lattice, store, collision): picks the pitch, sets the shared
 // memory size once per instantiation.  Returns the CUDA error of the launch.
-template <class L, int SK, int COLL, int PITCH, bool WIDE>
-int launch_tma_variant(const CUtensorMap& map, const StepArgs& a, bool fullbc, int rows, int box, int* err,
-                       cudaStream_t s) {
-  const unsigned smem = tma_smem_bytes<L, PITCH>();
-  static const bool attr_full = cudaFuncSetAttribute(step_kernel_tma<L, SK, COLL, true, PITCH, WIDE>,
-                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, smem) == cudaSuccess;
-  static const bool attr_part = cudaFuncSetAttribute(step_kernel_tma<L, SK, COLL, false, PITCH, WIDE>,
-                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, smem) == cudaSuccess;
-  if (!attr_full || !attr_part) return (int)cudaErrorInvalidValue;
+template <class L, int SK, int COLL, bool FULLBC, int PITCH, bool WIDE, bool DIAG>
+int launch_tma_kernel(const CUtensorMap& map, const StepArgs& a, int rows, int box, int* err, cudaStream_t s) {
+  constexpr int EB = sizeof(typename Store<SK, float>::Bits);
+  const unsigned smem = tma_smem_bytes<L, EB, PITCH>();
+  static const bool attr = cudaFuncSetAttribute(step_kernel_tma<L, SK, COLL, FULLBC, PITCH, WIDE, DIAG>,
+                                                cudaFuncAttributeMaxDynamicSharedMemorySize, smem) == cudaSuccess;
+  if (!attr) return (int)cudaErrorInvalidValue;
   const dim3 grid((unsigned)a.n0, (unsigned)((a.n1 + rows - 1) / rows));
-  if (fullbc)
-    step_kernel_tma<L, SK, COLL, true, PITCH, WIDE>
-        <<<grid, tma_consumers<PITCH>() + 32, smem, s>>>(map, a, rows, box, err);
-  else
-    step_kernel_tma<L, SK, COLL, false, PITCH, WIDE>
-        <<<grid, tma_consumers<PITCH>() + 32, smem, s>>>(map, a, rows, box, err);
+  step_kernel_tma<L, SK, COLL, FULLBC, PITCH, WIDE, DIAG>
+      <<<grid, tma_consumers<PITCH>() + 32, smem, s>>>(map, a, rows, box, err);
   return (int)cudaGetLastError();
 }
 
-template <class L, int SK, int COLL, int PITCH>
-int launch_tma_pitch(const CUtensorMap& map, const StepArgs& a, bool fullbc, int rows, int box, int* err,
-                     cudaStream_t s) {
-  return a.wide ? launch_tma_variant<L, SK, COLL, PITCH, true>(map, a, fullbc, rows, box, err, s)
-                : launch_tma_variant<L, SK, COLL, PITCH, false>(map, a, fullbc, rows, box, err, s);
+// The BC code variant (fullbc), the diagnostics step (a.diag_slots set; always
+// with the full BC code) when the instantiation has it (WITH_DIAG), and the
+// plane-offset width (a.wide).
+template <class L, int SK, int COLL, int PITCH, bool WIDE, bool WITH_DIAG>
+int launch_tma_variant(const CUtensorMap& map, const StepArgs& a, bool fullbc, int rows, int box, int* err,
+                       cudaStream_t s) {
+  if constexpr (WITH_DIAG) {
+    if (a.diag_slots != nullptr) return launch_tma_kernel<L, SK, COLL, true, PITCH, WIDE, true>(map, a, rows, box, err, s);
+  }
+  if (fullbc) return launch_tma_kernel<L, SK, COLL, true, PITCH, WIDE, false>(map, a, rows, box, err, s);
+  return launch_tma_kernel<L, SK, COLL, false, PITCH, WIDE, false>(map, a, rows, box, err, s);
 }
 
-template <int LAT, int SK, int COLL>
+template <class L, int SK, int COLL, int PITCH, bool WITH_DIAG>
+int launch_tma_pitch(const CUtensorMap& map, const StepArgs& a, bool fullbc, int rows, int box, int* err,
+                     cudaStream_t s) {
+  return a.wide ? launch_tma_variant<L, SK, COLL, PITCH, true, WITH_DIAG>(map, a, fullbc, rows, box, err, s)
+                : launch_tma_variant<L, SK, COLL, PITCH, false, WITH_DIAG>(map, a, fullbc, rows, box, err, s);
+}
+
+// Staged-row width for a contiguous axis of n2 cells.  16-bit stores: 256, 512
+// or 1024 (992 consumers); 4-byte stores: 192, 256 or 512 (n2 <= 512).
+template <int EB>
+inline int tma_pitch_for(int n2) {
+  if (EB == 4) return n2 <= 192 ? 192 : (n2 <= 256 ? 256 : 512);
+  return n2 <= 256 ? 256 : (n2 <= 512 ? 512 : 1024);
+}
+
+template <int LAT, int SK, int COLL, bool WITH_DIAG = false>
 int launch_tma_t(const CUtensorMap& map, const StepArgs& a, bool fullbc, int rows, int box, int* err,
                  cudaStream_t s) {
   using L = Lattice<LAT>;
-  if (a.n2 <= 256) return launch_tma_pitch<L, SK, COLL, 256>(map, a, fullbc, rows, box, err, s);
-  if (a.n2 <= 512) return launch_tma_pitch<L, SK, COLL, 512>(map, a, fullbc, rows, box, err, s);
-  return launch_tma_pitch<L, SK, COLL, 1024>(map, a, fullbc, rows, box, err, s);
+  constexpr int EB = sizeof(typename Store<SK, float>::Bits);
+  const int pitch = tma_pitch_for<EB>(a.n2);
+  if constexpr (EB == 4) {
+    if (pitch == 192) return launch_tma_pitch<L, SK, COLL, 192, WITH_DIAG>(map, a, fullbc, rows, box, err, s);
+    if (pitch == 256) return launch_tma_pitch<L, SK, COLL, 256, WITH_DIAG>(map, a, fullbc, rows, box, err, s);
+    return launch_tma_pitch<L, SK, COLL, 512, WITH_DIAG>(map, a, fullbc, rows, box, err, s);
+  } else {
+    if (pitch == 256) return launch_tma_pitch<L, SK, COLL, 256, WITH_DIAG>(map, a, fullbc, rows, box, err, s);
+    if (pitch == 512) return launch_tma_pitch<L, SK, COLL, 512, WITH_DIAG>(map, a, fullbc, rows, box, err, s);
+    return launch_tma_pitch<L, SK, COLL, 1024, WITH_DIAG>(map, a, fullbc, rows, box, err, s);
+  }
 }
 
 // Per-lattice entry points (step_tma_*.cu): raw FP16 with XLB-order BGK (code 0),
@@ -311,5 +367,8 @@ int launch_step_tma_d3q19(const CUtensorMap& map, const StepArgs& a, int sk, int
                           int box, int* err, cudaStream_t s);
 int launch_step_tma_d3q27(const CUtensorMap& map, const StepArgs& a, int sk, int coll, bool fullbc, int rows,
                           int box, int* err, cudaStream_t s);
+// FP32 store, KBC, D3Q27, with the diagnostics step (step_tma_d3q27_kbc.cu).
+int launch_step_tma_d3q27_kbc32(const CUtensorMap& map, const StepArgs& a, bool fullbc, int rows, int box, int* err,
+                                cudaStream_t s);
 
 }  // namespace xlbg

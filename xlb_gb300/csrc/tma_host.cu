@@ -65,14 +65,18 @@ int* fault_ptr() {
 // the calls made with a.wide set).  Returns 1 when it does not apply (the caller
 // uses the marching kernel), else the status.
 int try_launch_tma(const xlbg_desc* d, const StepArgs& a, bool fullbc, bool diag, cudaStream_t s) {
-  if (diag || d->compute != XLBG_COMPUTE_F32) return 1;
+  if (d->compute != XLBG_COMPUTE_F32) return 1;
   const int sk = d->store;
   const int coll = d->collision;
-  const bool combo =
+  const bool h16 =
       (sk == SK_F16 && coll == XLBG_BGK) || ((sk == SK_F16S || sk == SK_BF16S) && coll == XLBG_BGK_SHIFTED);
-  if (!combo) return 1;
+  // FP32 D3Q27 KBC: the compute-heavy sphere-channel step, also with diagnostics
+  const bool kbc32 = sk == SK_F32 && coll == XLBG_KBC && d->lattice == XLBG_D3Q27;
+  if (!(h16 && !diag) && !kbc32) return 1;
   const int q = d->lattice == XLBG_D2Q9 ? 9 : (d->lattice == XLBG_D3Q19 ? 19 : 27);
-  if (a.n2 < 8 || a.n2 > 992 || a.n2 % 8 != 0) return 1;
+  const int eb = kbc32 ? 4 : 2;
+  // rows of 16-byte multiples, at most 992 (16-bit) / 512 (FP32) cells
+  if (a.n2 < 8 || a.n2 > (kbc32 ? 512 : 992) || (a.n2 * eb) % 16 != 0) return 1;
   if (a.ncell >= 0x7fffffffLL) return 1;
   if (reinterpret_cast<uintptr_t>(a.f0) % 16 != 0) return 1;
   EncodeTiledFn enc = encode_fn();
@@ -82,24 +86,26 @@ int try_launch_tma(const xlbg_desc* d, const StepArgs& a, bool fullbc, bool diag
   const int box = a.n2 < kTmaBox ? a.n2 : kTmaBox;
   CUtensorMap map;
   const cuuint64_t dims[4] = {(cuuint64_t)a.n2, (cuuint64_t)a.n1, (cuuint64_t)a.n0, (cuuint64_t)q};
-  const cuuint64_t strides[3] = {(cuuint64_t)a.n2 * 2, (cuuint64_t)a.n1 * a.n2 * 2, (cuuint64_t)a.ncell * 2};
+  const cuuint64_t strides[3] = {(cuuint64_t)a.n2 * eb, (cuuint64_t)a.n1 * a.n2 * eb, (cuuint64_t)a.ncell * eb};
   const cuuint32_t boxdim[4] = {(cuuint32_t)box, 1, 1, 1};
   const cuuint32_t estr[4] = {1, 1, 1, 1};
-  if (enc(&map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 4, const_cast<void*>(a.f0), dims, strides, boxdim, estr,
-          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+  if (enc(&map, eb == 4 ? CU_TENSOR_MAP_DATA_TYPE_UINT32 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 4, const_cast<void*>(a.f0),
+          dims, strides, boxdim, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+          CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
     return 1;
 
   // rows of axis 1 per CTA: about sixteen resident waves of CTAs over 152 SMs
   // (measured at 512^3: 54 rows 58.2, 108 rows 57.3, 27 rows 57.2 GLUPS)
-  const int cps = a.n2 <= 256 ? 4 : (a.n2 <= 512 ? 2 : 1);
+  const int cps = eb == 4 ? (a.n2 <= 256 ? 2 : 1) : (a.n2 <= 256 ? 4 : (a.n2 <= 512 ? 2 : 1));
   const long long target = 152LL * cps * 16;
   long long rows = ((long long)a.n0 * a.n1 + target - 1) / target;
   if (rows < 1) rows = 1;
   if (rows > a.n1) rows = a.n1;
 
   int r;
-  if (d->lattice == XLBG_D2Q9)
+  if (kbc32)
+    r = launch_step_tma_d3q27_kbc32(map, a, fullbc, (int)rows, box, err, s);
+  else if (d->lattice == XLBG_D2Q9)
     r = launch_step_tma_d2q9(map, a, sk, coll, fullbc, (int)rows, box, err, s);
   else if (d->lattice == XLBG_D3Q19)
     r = launch_step_tma_d3q19(map, a, sk, coll, fullbc, (int)rows, box, err, s);
