@@ -179,14 +179,6 @@ class Store:
             return (g + self._w(np.float32, g.ndim)).astype(np.float32)
         return g.astype(np.float16) if self.kind == "f16s" else _bf16_round(g)
 
-    def to_deviation(self, f):
-        """float32 f (q, ...) -> g = RN(scale f - scale w_l), one rounding (a fused multiply-add)."""
-        sw = (self.scale * self._w(np.float32, f.ndim)).astype(np.float32)
-        return fma32(f, self.scale, -sw)
-
-    def from_deviation(self, g):
-        """float32 g (q, ...) -> f = RN(g / scale + w_l), one rounding; equals decode()."""
-        return fma32(g, np.float32(1.0) / self.scale, self._w(np.float32, g.ndim))
 
 
 # ----------------------------------------------------------------------------
@@ -623,6 +615,67 @@ def zouhe_like(lat, f, miss, aux, kind, T):
     return out
 
 
+def equilibrium_dev(lat, drho, u, scale):
+    """scale (feq_l - w_l) from rho - 1 and u, without cancellation against 1
+    or w_l (collision code 3; the CUDA path's equilibrium_dev, FP32):
+    rho e_l - 1 = drho e_l + (e_l - 1), e_l - 1 = t + t^2/2 - 1.5|u|^2, t = 3 c_l.u."""
+    f32 = np.float32
+    usq = u[0] * u[0]
+    for d in range(1, lat.d):
+        usq = fma32(u[d], u[d], usq)
+    b = f32(-1.5) * usq
+    w = lat.w.astype(f32)
+    geq = []
+    for l in range(lat.q):
+        cu = np.zeros_like(usq)
+        for d in range(lat.d):
+            if lat.c[d, l] == 1:
+                cu = cu + u[d]
+            elif lat.c[d, l] == -1:
+                cu = cu - u[d]
+        t = f32(3.0) * cu
+        em1 = fma32(f32(0.5) * t, t, t + b)
+        e = f32(1.0) + em1
+        geq.append((f32(scale) * w[l]) * fma32(drho, e, em1))
+    return np.stack(geq)
+
+
+def zouhe_like_dev(lat, g, miss, aux, kind, scale):
+    """ZouHe / Regularized on deviations g = scale (f - w) (collision code 3,
+    FP32; the CUDA path's zouhe_like_dev).  XLB's fsum (helper_functions_bc.py:
+    236-248) is 1 + dW + G/scale with G the same selection summed over g and dW
+    the weights of directions missing together with their opposite; rho - 1 and
+    u follow from it as in bc_zouhe.py:279-343 without forming rho near 1."""
+    f32 = np.float32
+    K = f32(1.0) / f32(scale)
+    nv = normals_float(lat, miss, f32).astype(f32)
+    w = lat.w.astype(f32)
+    G = np.zeros_like(g[0])
+    dW = np.zeros_like(g[0])
+    for l in range(lat.q):
+        k = miss[lat.opp[l]]
+        m = (~k) & (~miss[l])
+        G = np.where(k, G + f32(2.0) * g[l], G)
+        G = np.where(m, G + g[l], G)
+        dW = np.where(k & miss[l], dW + w[l], dW)
+    fs1 = fma32(K, G, dW)
+    if kind.endswith("velocity"):
+        u = [(-aux) * nv[d] for d in range(lat.d)]
+        unormal = np.zeros_like(fs1)
+        for d in range(lat.d):
+            unormal = unormal + u[d] * nv[d]
+        drho = (fs1 - unormal) / (f32(1.0) + unormal)
+    else:
+        drho = aux - f32(1.0)
+        unormal = (fs1 - drho) / aux
+        u = [unormal * nv[d] for d in range(lat.d)]
+    geq = equilibrium_dev(lat, drho, u, scale)
+    g = bounceback_noneq(lat, g, geq, miss)
+    if kind.startswith("regularized"):
+        g = regularize(lat, g, geq, f32)
+    return g
+
+
 def extrapolation_cs(T):
     """cs = 1/sqrt(3) as XLB builds it: compute_dtype(1.0 / wp.sqrt(3.0))
     (bc_extrapolation_outflow.py:353); Warp evaluates wp.sqrt(3.0) at Python
@@ -743,10 +796,10 @@ def step(lat, store, f0, f1, bc_mask, missing, omega, bcs, collision="BGK", T=np
 
 def _step_shifted(lat, store, f0, f1, bc_mask, missing, omega, bcs, recovery):
     """step() with collision code 3 (shifted or FP32 stores, FP32): every pulled value,
-    streaming-step result and collision output is a stored deviation g.  The
+    streaming-step result and collision output is a deviation g.  The
     bounce-back kinds copy deviations (w_l = w_opp(l)), the extrapolation blend
     is the same linear expression on g, and EquilibriumBC / ZouHe / Regularized
-    run on f between one from_deviation and one to_deviation per direction."""
+    run on deviations (equilibrium_dev, zouhe_like_dev)."""
     if not (store.shifted or store.kind == "f32"):
         raise ValueError("BGK_SHIFTED needs a shifted or FP32 store")
     T = np.float32
@@ -768,12 +821,12 @@ def _step_shifted(lat, store, f0, f1, bc_mask, missing, omega, bcs, recovery):
             for l in range(lat.q):
                 gp[l] = np.where(miss[l], own[lat.opp[l]], gp[l])
         elif bc.kind == "equilibrium":
-            rho_bc = np.full(gp.shape[1], T(bc.rho), dtype=T)
+            drho = np.full(gp.shape[1], T(bc.rho - 1.0), dtype=T)
             u_bc = [np.full(gp.shape[1], T(bc.u[d]), dtype=T) for d in range(lat.d)]
-            gp = store.to_deviation(equilibrium(lat, rho_bc, u_bc, T))
+            gp = equilibrium_dev(lat, drho, u_bc, store.scale)
         else:
             aux = store.decode_raw(f1[0][m], T)
-            gp = store.to_deviation(zouhe_like(lat, store.from_deviation(gp), miss, aux, bc.kind, T))
+            gp = zouhe_like_dev(lat, gp, miss, aux, bc.kind, store.scale)
         gps[:, m] = gp
 
     gout = bgk_shifted(lat, gps, T(omega), store.scale)

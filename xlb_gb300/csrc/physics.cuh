@@ -391,4 +391,95 @@ __device__ __forceinline__ void zouhe_like(T (&f)[L::Q], uint32_t miss, T aux, i
   }
 }
 
+// The boundary functionals on stored deviations g = S (f - w) (collision code 3;
+// no XLB counterpart, the equations of quadratic_equilibrium.py:35-60,
+// bc_equilibrium.py:75-86 and helper_functions_bc.py:236-297 rewritten so that
+// rho - 1 and feq - w are formed without cancellation against 1 or w).
+//
+// Quadratic equilibrium as deviations: S (feq_l - w_l) = S w_l (rho e_l - 1) with
+// rho e_l - 1 = drho e_l + (e_l - 1), e_l - 1 = t + t^2/2 - 1.5 |u|^2, t = 3 c_l.u.
+template <class L, int SK>
+__device__ __forceinline__ void equilibrium_dev(float drho, const float (&u)[L::D], float (&geq)[L::Q]) {
+  constexpr float S = shift_scale<SK>();
+  float usq = u[0] * u[0];
+#pragma unroll
+  for (int d = 1; d < L::D; ++d) usq = __fmaf_rn(u[d], u[d], usq);
+  const float b = -1.5f * usq;
+#pragma unroll
+  for (int l = 0; l < L::Q; ++l) {
+    float cu = 0.0f;
+#pragma unroll
+    for (int d = 0; d < L::D; ++d) {
+      if (L::c(l, d) == 1) cu = cu + u[d];
+      if (L::c(l, d) == -1) cu = cu - u[d];
+    }
+    const float t = 3.0f * cu;
+    const float em1 = __fmaf_rn(0.5f * t, t, t + b);
+    const float e = 1.0f + em1;
+    geq[l] = (S * (float)weight<L>(l)) * __fmaf_rn(drho, e, em1);
+  }
+}
+
+// ZouHe / Regularized, velocity or pressure, on deviations.  XLB's
+// fsum = sum_{opp l missing} 2 f_l + sum_{l, opp l present} f_l equals
+// 1 + dW + G/S, G the same sum over g and dW the weights of the directions that
+// are missing together with their opposite (0 on a face), so
+//   velocity (u = -aux n, u.n = -aux): rho - 1 = (fsum - 1 - u.n) / (1 + u.n),
+//   pressure (rho = aux):              u.n = (fsum - 1 - (rho - 1)) / rho,
+// then the non-equilibrium bounce-back and the regularisation as in zouhe_like
+// (every step linear in g except through rho and u).
+template <class L, int SK>
+__device__ __forceinline__ void zouhe_like_dev(float (&g)[L::Q], uint32_t miss, float aux, int kind) {
+  constexpr float S = shift_scale<SK>();
+  constexpr float K = 1.0f / S;
+  int nv[L::D];
+  normal_of<L>(miss, nv);
+  float G = 0.0f, dW = 0.0f;
+#pragma unroll
+  for (int l = 0; l < L::Q; ++l) {
+    const bool k = (miss >> opp<L>(l)) & 1u;
+    const bool m = !k && !((miss >> l) & 1u);
+    if (k) G = G + 2.0f * g[l];
+    if (m) G = G + g[l];
+    if (k && ((miss >> l) & 1u)) dW = dW + (float)weight<L>(l);
+  }
+  const float fs1 = __fmaf_rn(K, G, dW);  // fsum - 1
+  float drho, u[L::D];
+  if (kind == BC_ZOUHE_V || kind == BC_REG_V) {
+    float unormal = 0.0f;
+#pragma unroll
+    for (int d = 0; d < L::D; ++d) u[d] = (-aux) * (float)nv[d];
+#pragma unroll
+    for (int d = 0; d < L::D; ++d) unormal = unormal + u[d] * (float)nv[d];
+    drho = (fs1 - unormal) / (1.0f + unormal);
+  } else {
+    drho = aux - 1.0f;
+    const float unormal = (fs1 - drho) / aux;
+#pragma unroll
+    for (int d = 0; d < L::D; ++d) u[d] = unormal * (float)nv[d];
+  }
+  float geq[L::Q];
+  equilibrium_dev<L, SK>(drho, u, geq);
+#pragma unroll
+  for (int l = 0; l < L::Q; ++l) {
+    if ((miss >> l) & 1u) g[l] = g[opp<L>(l)] + geq[l] - geq[opp<L>(l)];
+  }
+  if (kind == BC_REG_V || kind == BC_REG_P) {
+    float gneq[L::Q];
+#pragma unroll
+    for (int l = 0; l < L::Q; ++l) gneq[l] = g[l] - geq[l];
+    float pi[L::NT];
+    second_moment<L>(gneq, pi);
+#pragma unroll
+    for (int l = 0; l < L::Q; ++l) {
+      float acc = 0.0f;
+#pragma unroll
+      for (int t = 0; t < L::NT; ++t) {
+        if (qi<L>(l, t) != 0.0) acc = acc + (float)qi<L>(l, t) * pi[t];
+      }
+      g[l] = geq[l] + 4.5f * (float)weight<L>(l) * acc;
+    }
+  }
+}
+
 }  // namespace xlbg

@@ -187,10 +187,10 @@ __device__ __forceinline__ void store_cell(const StepArgs& a, Idx cell, const T 
 // Everything after the pull for one cell: BC lookup, streaming-step BC,
 // collision, collision-step BC, store to f1 and the diagnostics contributions.
 // f holds the pulled values of the cell; the cell is not a skip cell (id 255).
-// With collision code 3 every value in f and fo is a stored deviation g: the
+// With collision code 3 every value in f and fo is a deviation g: the
 // bounce-back kinds copy deviations (w_l = w_opp l), the extrapolation blend is
-// linear, and EquilibriumBC / ZouHe / Regularized run in f (XLB's order) between
-// one from_dev / to_dev per direction.
+// linear, and EquilibriumBC / ZouHe / Regularized run on deviations too
+// (equilibrium_dev, zouhe_like_dev).
 // The collision is inlined once, shared by fluid and boundary cells (a second
 // copy for a fluid-only path doubled the code and ran slower).
 template <class L, int SK, class T, int COLL, bool FULLBC, bool DIAG, class Idx>
@@ -225,23 +225,17 @@ __device__ __forceinline__ void cell_update(const StepArgs& a, int i0, int i1, i
       T u[L::D];
 #pragma unroll
       for (int d = 0; d < L::D; ++d) u[d] = T(a.bc[slot].u[d]);
-      equilibrium<L>(T(a.bc[slot].rho), u, f);
-      if constexpr (COLL == 3) {
-#pragma unroll
-        for (int l = 0; l < Q; ++l) f[l] = St::to_dev(f[l], T(weight<L>(l)));
-      }
+      if constexpr (COLL == 3)
+        equilibrium_dev<L, SK>((float)(a.bc[slot].rho - 1.0), u, f);
+      else
+        equilibrium<L>(T(a.bc[slot].rho), u, f);
     } else if (FULLBC && kind >= BC_ZOUHE_V && kind <= BC_REG_P) {
       // the prescribed value lives in slot 0 of f1 (boundary_condition.py:151-152)
       const T aux = St::dec_raw(static_cast<const Bits*>(a.aux)[cell]);
-      if constexpr (COLL == 3) {
-#pragma unroll
-        for (int l = 0; l < Q; ++l) f[l] = St::from_dev(f[l], T(weight<L>(l)));
-      }
-      zouhe_like<L>(f, miss, aux, kind);
-      if constexpr (COLL == 3) {
-#pragma unroll
-        for (int l = 0; l < Q; ++l) f[l] = St::to_dev(f[l], T(weight<L>(l)));
-      }
+      if constexpr (COLL == 3)
+        zouhe_like_dev<L, SK>(f, miss, aux, kind);
+      else
+        zouhe_like<L>(f, miss, aux, kind);
     }
   }
 

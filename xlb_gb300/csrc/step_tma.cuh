@@ -261,7 +261,15 @@ __global__ void __launch_bounds__(tma_consumers<PITCH>() + 32,
     }
     __syncwarp();
     if (lane == 0) mbar_arrive(empty + 8 * s);
-    if constexpr (DIAG) {
+    if (__all_sync(0xffffffffu, id == 0)) {
+      // every cell of the warp is fluid (lanes past the row carry id 255): the
+      // collision and the store alone, which is what cell_update does for id 0
+      T fo[Q];
+      collide<L, SK, T, COLL>(f, omega_of<T>(a), fo);
+      double dmc = 0.0;
+      store_cell<L, SK, T, COLL, DIAG>(a, (Idx)cell, fo, dmc);
+      if constexpr (DIAG) dm += dmc;
+    } else if constexpr (DIAG) {
       if (id != 255) {
         double dmc = 0.0, dfc[3] = {0.0, 0.0, 0.0};
         cell_update<L, SK, T, COLL, FULLBC, true>(a, i0, y, i2, (Idx)cell, id, f, dmc, dfc);

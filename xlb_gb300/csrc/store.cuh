@@ -29,8 +29,6 @@ struct Store<SK_F32, T> {
   // w_l / 2 <= f <= 2 w_l (Sterbenz); the store rounds f = w_l + g once
   __device__ static __forceinline__ T dev(Bits b, T w) { return __uint_as_float(b) - w; }
   __device__ static __forceinline__ Bits enc_dev(T g, T w) { return __float_as_uint(g + w); }
-  __device__ static __forceinline__ T to_dev(T v, T w) { return v - w; }
-  __device__ static __forceinline__ T from_dev(T g, T w) { return g + w; }
 };
 
 template <class T>
@@ -64,10 +62,7 @@ struct Store<SK_F16, T> {
 //
 // The shifted forms also expose the stored deviation itself, g = kScale (f - w),
 // for the collision evaluated on deviations (collision code 3): dev / enc_dev
-// convert between the stored bits and g (one conversion each way; w unused),
-// to_dev / from_dev between g and f (one fused multiply-add each way;
-// dec(b, w) == from_dev(dev(b, w), w) and enc(v, w) == enc_dev(to_dev(v, w), w)
-// bit for bit).
+// convert between the stored bits and g (one conversion each way; w unused).
 template <>
 struct Store<SK_F16S, float> {
   using S = __half;
@@ -84,8 +79,6 @@ struct Store<SK_F16S, float> {
   __device__ static __forceinline__ float dec_raw(Bits b) { return __half2float(__ushort_as_half(b)); }
   __device__ static __forceinline__ float dev(Bits b, float) { return __half2float(__ushort_as_half(b)); }
   __device__ static __forceinline__ Bits enc_dev(float g, float) { return __half_as_ushort(__float2half_rn(g)); }
-  __device__ static __forceinline__ float to_dev(float v, float w) { return __fmaf_rn(v, kScale, -(w * kScale)); }
-  __device__ static __forceinline__ float from_dev(float g, float w) { return __fmaf_rn(g, kInvScale, w); }
 };
 
 template <>
@@ -106,8 +99,6 @@ struct Store<SK_BF16S, float> {
   __device__ static __forceinline__ Bits enc_dev(float g, float) {
     return __bfloat16_as_ushort(__float2bfloat16_rn(g));
   }
-  __device__ static __forceinline__ float to_dev(float v, float w) { return v - w; }
-  __device__ static __forceinline__ float from_dev(float g, float w) { return g + w; }
 };
 
 // A pulled population as the collision code works on it: f for codes 0-2, the

@@ -102,9 +102,26 @@ class SlabFields:
         self.f_0, self.f_1 = self.f_1, self.f_0
 
 
+def _as_slice(dirs):
+    """The direction list as a slice when it is an arithmetic progression (it is
+    for XLB's orderings: D3Q19 14..18 / 9..13, D3Q27 18..26 / 9..17, D2Q9 3,5,7 /
+    4,6,8), else None."""
+    if len(dirs) == 1:
+        return slice(dirs[0], dirs[0] + 1)
+    step = dirs[1] - dirs[0]
+    if step > 0 and all(b - a == step for a, b in zip(dirs, dirs[1:])):
+        return slice(dirs[0], dirs[-1] + 1, step)
+    return None
+
+
 def _plane_copy(dst, dst_plane, src, src_plane, dirs):
-    """dst[dirs, dst_plane] = src[dirs, src_plane] for a list of directions
-    (each (l, plane) block is contiguous in the (Q, x, ...) layout)."""
+    """dst[dirs, dst_plane] = src[dirs, src_plane]: one strided copy when the
+    directions are evenly spaced, else one copy per direction (each (l, plane)
+    block is contiguous in the (Q, x, ...) layout)."""
+    sl = _as_slice(dirs)
+    if sl is not None:
+        dst[sl, dst_plane].copy_(src[sl, src_plane], non_blocking=True)
+        return
     for l in dirs:
         dst[l, dst_plane].copy_(src[l, src_plane], non_blocking=True)
 
@@ -161,8 +178,9 @@ class ProcessGroupTransport:
             _plane_copy(s.f_0, s.t + 1, s.f_0, 1, left)
             return
         dist = self.dist
-        send_r = torch.stack([s.f_0[l, s.t] for l in right])
-        send_l = torch.stack([s.f_0[l, 1] for l in left])
+        sr, sl = _as_slice(right), _as_slice(left)
+        send_r = s.f_0[sr, s.t].contiguous() if sr is not None else torch.stack([s.f_0[l, s.t] for l in right])
+        send_l = s.f_0[sl, 1].contiguous() if sl is not None else torch.stack([s.f_0[l, 1] for l in left])
         recv_l = torch.empty_like(send_r)
         recv_r = torch.empty_like(send_l)
         prev = dist.get_global_rank(self.group, (self.rank - 1) % self.size) if self.group else (self.rank - 1) % self.size
@@ -175,10 +193,16 @@ class ProcessGroupTransport:
         ]
         for req in dist.batch_isend_irecv(ops):
             req.wait()
-        for k, l in enumerate(right):
-            s.f_0[l, 0].copy_(recv_l[k])
-        for k, l in enumerate(left):
-            s.f_0[l, s.t + 1].copy_(recv_r[k])
+        if sr is not None:
+            s.f_0[sr, 0].copy_(recv_l)
+        else:
+            for k, l in enumerate(right):
+                s.f_0[l, 0].copy_(recv_l[k])
+        if sl is not None:
+            s.f_0[sl, s.t + 1].copy_(recv_r)
+        else:
+            for k, l in enumerate(left):
+                s.f_0[l, s.t + 1].copy_(recv_r[k])
 
     def all_reduce(self, t):
         self.dist.all_reduce(t, group=self.group)
