@@ -16,7 +16,8 @@ Set-up, in 2D (D2Q9, 512 x 128) or 3D (D3Q19, 128^3):
 Reported: forward and backward time (CUDA events), their ratio, peak device
 memory, and the gradient error against FP64 central finite differences along
 a seeded random direction of the amplitudes (FP64FP64 runs), for the FP32
-adjoint and for the FP64 adjoint.
+adjoint (forward as BGK on deviations from rest, collision_type "BGK_SHIFTED";
+and with XLB's BGK order for comparison) and for the FP64 adjoint.
 
 Run directly (``python bench_adjoint.py --dim 2``) for one JSON line, or call
 ``measure`` from bench.py.
@@ -119,7 +120,7 @@ def measure_fp32(dim=2, steps=None):
     """The FP32 forward + backward only (target from an FP32 run), for profiling."""
     steps = steps or (2000 if dim == 2 else 500)
     dev = torch.device("cuda")
-    ctx = _build(dim, "FP32FP32", steps)
+    ctx = _build(dim, "FP32FP32", steps, collision="BGK_SHIFTED")
     ny = ctx["ny"]
     y = torch.arange(ny, dtype=torch.float32, device=dev)
     c32 = _c_matrix(ctx["stepper"], torch.float32, dev)
@@ -173,8 +174,9 @@ def measure(dim=2, steps=None, h=1e-5, fd=True):
     del ctx64, f64, amp64, f_t
     torch.cuda.empty_cache()
 
-    # FP32 side: the timed forward + backward
-    ctx = _build(dim, "FP32FP32", steps)
+    # FP32 side: the timed forward + backward, BGK on deviations from rest (the
+    # FP32 form whose sums do not cancel; XLB's BGK order is graded below)
+    ctx = _build(dim, "FP32FP32", steps, collision="BGK_SHIFTED")
     c32 = _c_matrix(ctx["stepper"], torch.float32, dev)
     loss32 = _loss_fn(ctx, c32, u_target.float())
 
@@ -213,6 +215,18 @@ def measure(dim=2, steps=None, h=1e-5, fd=True):
     })
     if fd:
         out["grad32_rel_err_vs_fd64"] = abs(float(g32 @ v) - out["fd64_directional"]) / abs(out["fd64_directional"])
+    del ctx
+    torch.cuda.empty_cache()
+    # FP32 with XLB's BGK operation order: the same adjoint, the forward summing f ~ w
+    ctx = _build(dim, "FP32FP32", steps)
+    loss = _loss_fn(ctx, _c_matrix(ctx["stepper"], torch.float32, dev), u_target.float())
+    amp = torch.ones(ny, dtype=torch.float32, device=dev, requires_grad=True)
+    loss(ctx["f_0"].clone().requires_grad_(True), amp).backward()
+    gx = amp.grad.detach().double()
+    out["grad32_xlb_order_rel_l2_vs_grad64"] = float(torch.linalg.norm(gx - g64) / torch.linalg.norm(g64))
+    if fd:
+        out["grad32_xlb_order_rel_err_vs_fd64"] = abs(float(gx @ v) - out["fd64_directional"]) / abs(
+            out["fd64_directional"])
     del ctx
     torch.cuda.empty_cache()
     # FP32 store with FP64 arithmetic: separates storage rounding from arithmetic rounding

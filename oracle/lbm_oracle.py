@@ -432,7 +432,9 @@ def bgk_shifted(lat, g, omega_t, scale):
     form, rewritten for g:
       rho = 1 + G/scale, v = 3u = 3 J/(scale rho), base = 1 - |v|^2/6,
       r = rho base - 1 = (G/scale) base - |v|^2/6 (no cancellation),
-      per weight class k: A = omega scale w_k, C = A r,
+      per weight class k: A = omega scale w_k (two floats hi + lo: a rounded A
+        is a systematic error of the class that breaks momentum conservation),
+        A rho and C = A r each rounded once,
       per pair (l, o) with t = c_l.v: R = C + (A rho / 2) t^2,
       g_out_l = (1 - omega) g_l + (A rho t + R), g_out_o = (1 - omega) g_o + (-A rho t + R).
     FP32 only; the operation order (and every fused multiply-add, fma32) is the
@@ -466,12 +468,17 @@ def bgk_shifted(lat, g, omega_t, scale):
     omf = f32(1.0) - f32(omega_t)
     norm1 = np.abs(lat.c).sum(axis=0)
     Ar, Arh, C = {}, {}, {}
+    om = f32(omega_t)
     for k in sorted(set(norm1.tolist())):
-        wk = lat.w[int(np.argmax(norm1 == k))].astype(np.float32)
-        A = f32(omega_t) * (S * wk)
-        Ar[k] = A * rho
+        # A = omega S w_k carried as hi + lo (S w_k split into two floats in float64)
+        sw = float(S) * float(lat.w[int(np.argmax(norm1 == k))])
+        whi = f32(sw)
+        wlo = f32(sw - float(whi))
+        ahi = om * whi
+        alo = fma32(om, whi, -ahi) + om * wlo
+        Ar[k] = fma32(ahi, rho, alo * rho)
         Arh[k] = f32(0.5) * Ar[k]
-        C[k] = A * r
+        C[k] = fma32(ahi, r, alo * r)
     go = np.empty_like(g)
     go[0] = fma32(omf, g[0], C[0])
     for l in pairs:

@@ -1,4 +1,4 @@
-"""Workload-size checks.
+"""Workload-size checks: C1 at full size, C3 at a reduced size.
 
 C1: the 2D lid-driven cavity at its full size -- D2Q9 BGK 256 x 256, FullwayBB on
 the left, right and bottom walls, EquilibriumBC lid (rho 1, u = (0.05, 0)) on the
@@ -59,3 +59,59 @@ def test_c1_fp32_close_to_fp64_oracle(c1_oracle):
     assert err_u < 1e-3, msg
     assert err_rho < 1e-4, msg
     assert err_m < 1e-4, msg
+
+
+# C3 reduced: the sphere-channel layout of the D3Q27 KBC external-flow workload
+# (FullwayBB side walls, Regularized velocity inlet 0.04 +-1 % per cell,
+# ExtrapolationOutflow, HalfwayBB sphere) on 192 x 48 x 48 cells with the
+# workload's omega (Re 1000 on a 48-cell sphere: nu = 0.04 * 48 / 1000).
+C3R_SHAPE = (192, 48, 48)
+C3R_OMEGA = 1.0 / (3.0 * (0.04 * 48 / 1000.0) + 0.5)
+
+
+@pytest.fixture(scope="module")
+def c3r_oracles():
+    out = {}
+    for policy, T in (("fp32", np.float32), ("fp64", np.float64)):
+        sc = Scenario("D3Q27", C3R_SHAPE, "channel_regularized", policy, "KBC", omega=C3R_OMEGA)
+        st = cref.Stepper(sc.lat, sc.shape, sc.bc_mask, sc.missing, sc.obcs, "KBC", T, threads=0)
+        out[policy] = st.run(sc.f0.copy(), sc.f1.copy(), C3R_OMEGA, 200)
+    return out
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("policy", ["fp32", "fp64"])
+def test_c3_reduced_equals_c_oracle(c3r_oracles, policy):
+    """200 steps of the reduced sphere channel (FP32: the TMA-staged KBC kernel;
+    FP64: the marching kernel) equal the C restatement bit for bit."""
+    want0, want1 = c3r_oracles[policy]
+    sc = Scenario("D3Q27", C3R_SHAPE, "channel_regularized", policy, "KBC", omega=C3R_OMEGA)
+    got0, got1 = sc.gpu_steps(200, use_run=True)
+    np.testing.assert_array_equal(got0, want0)
+    np.testing.assert_array_equal(got1, want1)
+
+
+@pytest.mark.gpu
+def test_c3_reduced_fp32_close_to_fp64():
+    """FP32 against FP64 after 1000 steps of the reduced sphere channel (the FP64
+    path equals the oracle bit for bit, above): velocity 1e-4 and density 1e-5
+    relative L2 over the fluid cells, drag and lift (MomentumTransfer on the
+    final state) 1e-3 of the drag."""
+    from xlb_gb300.operator.force import MomentumTransfer
+
+    res = {}
+    for policy in ("fp64", "fp32"):
+        sc = Scenario("D3Q27", C3R_SHAPE, "channel_regularized", policy, "KBC", omega=C3R_OMEGA)
+        f_0, f_1, bcm, mm = sc.gpu_fields()
+        f_0, f_1 = sc.stepper.run(f_0, f_1, bcm, mm, sc.omega, 1000)
+        force = MomentumTransfer(sc.xbcs[3])(f_0, f_1, bcm, mm)
+        rho, u = _rho_u(sc.lat, sc.to_numpy(f_0))
+        fluid = sc.bc_mask.reshape(-1) == 0
+        res[policy] = (rho[fluid], u[:, fluid], force)
+    (r64, u64, F64), (r32, u32, F32) = res["fp64"], res["fp32"]
+    err_u = np.linalg.norm(u32 - u64) / np.linalg.norm(u64)
+    err_rho = np.linalg.norm(r32 - r64) / np.linalg.norm(r64)
+    err_f = np.max(np.abs(F32 - F64)) / abs(F64[0])
+    msg = f"u {err_u:.3e} rho {err_rho:.3e} force {err_f:.3e} (F64 {F64}, F32 {F32})"
+    assert np.all(np.isfinite(u32)) and abs(F64[0]) > 0, msg
+    assert err_u < 1e-4 and err_rho < 1e-5 and err_f < 1e-3, msg

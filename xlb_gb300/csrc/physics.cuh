@@ -230,8 +230,8 @@ __device__ __forceinline__ void bgk_pair(const T (&f)[L::Q], T omega, T (&fo)[L:
 //   S (feq_l - w_l) = S w_l (rho e_l - 1),  e_l = 1 + t + t^2 / 2 - 1.5 |u|^2,  t = 3 c_l.u,
 //   g_out = (1 - omega) g + omega S (feq - w).
 // Over an opposite pair (l, o) t changes sign; with A = omega S w (one per
-// weight class), v = 3u, base = 1 - |v|^2 / 6, C = A (rho base - 1) and
-// R = C + (A rho / 2) t^2:
+// weight class, carried in two floats), v = 3u, base = 1 - |v|^2 / 6,
+// C = A (rho base - 1) and R = C + (A rho / 2) t^2:
 //   g_out_l = fma(1 - omega, g_l, fma( A rho, t, R)),
 //   g_out_o = fma(1 - omega, g_o, fma(-A rho, t, R)).
 // About 125 floating-point operations per D3Q19 cell, decode and encode
@@ -291,17 +291,24 @@ __device__ __forceinline__ void bgk_shifted(const float (&g)[L::Q], float omega,
   const float r = __fmaf_rn(K * G, base, bm1);
   const float omf = 1.0f - omega;
   float Ar[4] = {0.0f, 0.0f, 0.0f, 0.0f}, Arh[4] = {0.0f, 0.0f, 0.0f, 0.0f}, C[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-  // the class weights as compile-time constants (class_weight called with the
-  // unrolled index below would not be a constant expression and ran as a loop)
-  constexpr float Sw[4] = {S * (float)class_weight<L>(0), S * (float)class_weight<L>(1),
-                           S * (float)class_weight<L>(2), S * (float)class_weight<L>(3)};
+  // S w_k as a float pair hi + lo (compile-time constants; class_weight called with
+  // the unrolled index below would not be a constant expression and ran as a loop)
+  constexpr double Sw[4] = {(double)S * class_weight<L>(0), (double)S * class_weight<L>(1),
+                            (double)S * class_weight<L>(2), (double)S * class_weight<L>(3)};
+  constexpr float Whi[4] = {(float)Sw[0], (float)Sw[1], (float)Sw[2], (float)Sw[3]};
+  constexpr float Wlo[4] = {(float)(Sw[0] - (double)Whi[0]), (float)(Sw[1] - (double)Whi[1]),
+                            (float)(Sw[2] - (double)Whi[2]), (float)(Sw[3] - (double)Whi[3])};
 #pragma unroll
   for (int k = 0; k <= L::D; ++k) {
-    // weight class |c|_1 = k (D2Q9 and D3Q19 have no k = 3; the unused entries fold away)
-    const float A = omega * Sw[k];
-    Ar[k] = A * rho;
+    // weight class |c|_1 = k (D2Q9 and D3Q19 have no k = 3; the unused entries fold away).
+    // A = omega S w_k is carried as hi + lo: a rounded A is the same relative error
+    // in every cell and step of a class, which breaks the collision's exact
+    // momentum and mass balance and accumulates; A rho and A r are each rounded once.
+    const float Ahi = omega * Whi[k];
+    const float Alo = __fmaf_rn(omega, Whi[k], -Ahi) + omega * Wlo[k];
+    Ar[k] = __fmaf_rn(Ahi, rho, Alo * rho);
     Arh[k] = 0.5f * Ar[k];
-    C[k] = A * r;
+    C[k] = __fmaf_rn(Ahi, r, Alo * r);
   }
   go[0] = __fmaf_rn(omf, g[0], C[0]);
   shifted_pair_update<L, 0>(g, v, Ar, Arh, C, omf, go);

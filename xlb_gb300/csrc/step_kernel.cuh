@@ -184,6 +184,30 @@ __device__ __forceinline__ void store_cell(const StepArgs& a, Idx cell, const T 
   if constexpr (DIAG) dmass = (double)msum;
 }
 
+// The same store for a cell index below 2^31 (the TMA-staged kernel's fluid
+// path): each direction's plane base is launch-uniform and the cell index 32-bit,
+// so an address is one wide multiply-add of the cell index onto the plane base
+// rather than a 64-bit add to a per-cell pointer.
+template <class L, int SK, class T, int COLL, bool DIAG>
+__device__ __forceinline__ void store_cell_u32(const StepArgs& a, unsigned cell, const T (&fo)[L::Q],
+                                               double& dmass) {
+  using St = Store<SK, T>;
+  using Bits = typename St::Bits;
+  T msum = T(0);
+  const size_t plane = (size_t)a.ncell;
+#pragma unroll
+  for (int l = 0; l < L::Q; ++l) {
+    const Bits b = store_pop<SK, T, COLL>(fo[l], T(weight<L>(l)));
+    Bits* __restrict__ base = static_cast<Bits*>(a.f1) + (size_t)l * plane;
+    base[cell] = b;
+    if constexpr (DIAG) {
+      const T v = St::dec(b, T(weight<L>(l)));
+      msum = l == 0 ? v : msum + v;
+    }
+  }
+  if constexpr (DIAG) dmass = (double)msum;
+}
+
 // Everything after the pull for one cell: BC lookup, streaming-step BC,
 // collision, collision-step BC, store to f1 and the diagnostics contributions.
 // f holds the pulled values of the cell; the cell is not a skip cell (id 255).

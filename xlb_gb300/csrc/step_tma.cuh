@@ -267,7 +267,7 @@ __global__ void __launch_bounds__(tma_consumers<PITCH>() + 32,
       T fo[Q];
       collide<L, SK, T, COLL>(f, omega_of<T>(a), fo);
       double dmc = 0.0;
-      store_cell<L, SK, T, COLL, DIAG>(a, (Idx)cell, fo, dmc);
+      store_cell_u32<L, SK, T, COLL, DIAG>(a, cell, fo, dmc);
       if constexpr (DIAG) dm += dmc;
     } else if constexpr (DIAG) {
       if (id != 255) {
