@@ -442,7 +442,8 @@ def main():
         forms = {}
         del fields, stepper
         torch.cuda.empty_cache()
-        for name, pol in (("fp16_shifted", "FP32FP16S"), ("bf16_shifted", "FP32BF16S")):
+        for name, pol in (("fp16_shifted", "FP32FP16S"), ("bf16_shifted", "FP32BF16S"),
+                          ("fp16_shifted_sr", "FP32FP16SR"), ("bf16_shifted_sr", "FP32BF16SR")):
             st, fl, om = cavity_setup(n, pol)
             ms2, fl = timed_device(st, fl, om, args.steps, args.warmup)
             ms2 = max_over_ranks(ms2)

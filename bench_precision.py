@@ -4,7 +4,8 @@ in accuracy.
 D3Q19 BGK cavity (FullwayBB on five faces, EquilibriumBC lid u = (0.05, 0, 0)),
 Re = 200 with the characteristic length n - 1 (nu = 0.05 (n - 1) / 200,
 omega = 1 / (3 nu + 0.5)), initial state rest equilibrium.  Populations stored
-as FP32, FP16 (raw), FP16 shifted (f - w_l) and BF16 shifted, computed in FP32.
+as FP32, FP16 (raw), FP16 shifted (f - w_l) and BF16 shifted, the shifted forms
+also with stochastic rounding of the stores, all computed in FP32.
 
 * Error, at 256^3 after ``--steps`` (default 10 000) steps: relative L2 of the
   velocity over the fluid cells against FP64FP64 (this library's FP64 path,
@@ -24,7 +25,8 @@ import torch
 
 from bench import cavity_setup
 
-FORMS = [("fp32", "FP32FP32"), ("fp16", "FP32FP16"), ("fp16_shifted", "FP32FP16S"), ("bf16_shifted", "FP32BF16S")]
+FORMS = [("fp32", "FP32FP32"), ("fp16", "FP32FP16"), ("fp16_shifted", "FP32FP16S"), ("bf16_shifted", "FP32BF16S"),
+         ("fp16_shifted_sr", "FP32FP16SR"), ("bf16_shifted_sr", "FP32BF16SR")]
 
 
 def _omega(n):

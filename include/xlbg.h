@@ -58,8 +58,11 @@ enum { XLBG_COMPUTE_F32 = 0, XLBG_COMPUTE_F64 = 1 };
    shifted stores (XLBG_STORE_F16S / XLBG_STORE_BF16S; one conversion per pulled
    and per stored value), or f - w_l for XLBG_STORE_F32 (exact on load, one
    rounding on store), all with FP32 compute.  Sums of deviations do not cancel
-   the way sums of f ~ w_l do.  No XLB counterpart for 2 and 3. */
-enum { XLBG_BGK = 0, XLBG_KBC = 1, XLBG_BGK_PAIR = 2, XLBG_BGK_SHIFTED = 3 };
+   the way sums of f ~ w_l do.  XLBG_BGK_SHIFTED_SR is XLBG_BGK_SHIFTED on the
+   shifted 16-bit stores with stochastic rounding of every store (cvt.rs; random
+   bits from a hash of the cell index and the step's timestep argument, so runs
+   are reproducible).  No XLB counterpart for 2, 3 and 4. */
+enum { XLBG_BGK = 0, XLBG_KBC = 1, XLBG_BGK_PAIR = 2, XLBG_BGK_SHIFTED = 3, XLBG_BGK_SHIFTED_SR = 4 };
 
 /* boundary-condition kinds (xlb/operator/boundary_condition/bc_*.py) */
 enum {
@@ -90,7 +93,7 @@ typedef struct {
   int32_t lattice;     /* XLBG_D2Q9 / XLBG_D3Q19 / XLBG_D3Q27 */
   int32_t store;       /* XLBG_STORE_* */
   int32_t compute;     /* XLBG_COMPUTE_* */
-  int32_t collision;   /* XLBG_BGK / XLBG_KBC / XLBG_BGK_PAIR / XLBG_BGK_SHIFTED */
+  int32_t collision;   /* XLBG_BGK / XLBG_KBC / XLBG_BGK_PAIR / XLBG_BGK_SHIFTED(_SR) */
   int32_t nbc;         /* entries used in bc[] */
   int64_t nx, ny, nz;  /* grid shape; nz = 1 for 2D */
   xlbg_bc bc[XLBG_MAX_BC];

@@ -711,7 +711,8 @@ def _recovered(lat, f0, f1, bc_mask, missing, bcs, with_slot0=True):
     return out
 
 
-def step(lat, store, f0, f1, bc_mask, missing, omega, bcs, collision="BGK", T=np.float64, recovery="after"):
+def step(lat, store, f0, f1, bc_mask, missing, omega, bcs, collision="BGK", T=np.float64, recovery="after",
+         timestep=0):
     """One fused step.  Returns (f0_new, f1_new) as stored arrays.
 
     f0_new differs from f0 only where aux recovery wrote it
@@ -724,8 +725,9 @@ def step(lat, store, f0, f1, bc_mask, missing, omega, bcs, collision="BGK", T=np
     the recovered slots, which is what a launch gives when the ZouHe /
     Regularized cells run before the cells reading them.
     """
-    if collision == "BGK_SHIFTED":
-        return _step_shifted(lat, store, f0, f1, bc_mask, missing, omega, bcs, recovery)
+    if collision in ("BGK_SHIFTED", "BGK_SHIFTED_SR"):
+        return _step_shifted(lat, store, f0, f1, bc_mask, missing, omega, bcs, recovery,
+                             stochastic=collision == "BGK_SHIFTED_SR", timestep=timestep)
     shp = f0.shape[1:]
     ids = bc_mask[0]
     f0c = store.decode(f0, T)
@@ -801,7 +803,68 @@ def step(lat, store, f0, f1, bc_mask, missing, omega, bcs, collision="BGK", T=np
     return _recovered(lat, f0, f1, bc_mask, missing, bcs), f1_new
 
 
-def _step_shifted(lat, store, f0, f1, bc_mask, missing, omega, bcs, recovery):
+def sr_seed(cell, t):
+    """Random bits of one cell's stochastic rounding (collision code 4): the
+    "lowbias32" integer hash (C. Wellons) of cell * 0x9E3779B1 + t * 0x85EBCA77,
+    uint32 arithmetic as the CUDA path's sr_seed."""
+    x = np.asarray(cell, dtype=np.uint64).astype(np.uint32) * np.uint32(0x9E3779B1) + np.uint32(
+        (int(t) * 0x85EBCA77) & 0xFFFFFFFF)
+    x = x ^ (x >> np.uint32(16))
+    x = x * np.uint32(0x7FEB352D)
+    x = x ^ (x >> np.uint32(15))
+    x = x * np.uint32(0x846CA68B)
+    return x ^ (x >> np.uint32(16))
+
+
+def sr_bits(seed, k):
+    return seed * np.uint32(((2 * k + 1) * 0x9E3779B9) & 0xFFFFFFFF)
+
+
+def sr_round_f16(x, r16):
+    """Blackwell's cvt.rs to FP16 of float32 x with 16 random bits r16 (the CUDA
+    path's sr_pack, pinned on the GPU bit for bit): floor(|x| / ulp + r13 / 2^13)
+    ulp with r13 = r16 & 0x1FFF and ulp the FP16 ulp of |x|'s binade (2^-24 below
+    2^-14), signed; +-inf from 65536 up.  Returns the FP16 bits."""
+    x = np.asarray(x, dtype=np.float32)
+    ax = np.abs(x.astype(np.float64))
+    e = np.floor(np.log2(np.where(ax > 0, ax, 1.0)))
+    ulp = np.where(ax < 2.0**-14, 2.0**-24, 2.0 ** (e - 10))
+    v = ax / ulp
+    k = np.floor(v)
+    q = k + ((v - k) + (np.asarray(r16).astype(np.uint32) & np.uint32(0x1FFF)).astype(np.float64) / 8192.0 >= 1.0)
+    val = q * ulp
+    with np.errstate(over="ignore"):
+        h = np.where(val >= 65536.0, np.inf, val).astype(np.float16)
+    h = np.where(np.signbit(x), -h, h).astype(np.float16)
+    return h.view(np.uint16)
+
+
+def sr_round_bf16(x, r16):
+    """cvt.rs to BF16: the 16 random bits added to the low half of x's float32
+    pattern, then truncated to the upper half.  Returns the BF16 bits."""
+    b = np.ascontiguousarray(x, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    return ((b + (np.asarray(r16).astype(np.uint64) & 0xFFFF)) >> 16).astype(np.uint16)
+
+
+def encode_stochastic(store, g, timestep):
+    """Stored bits of deviations g (q, *shape) with stochastic rounding: pairs of
+    directions (2k, 2k + 1) share one 32-bit word of random bits, the lower
+    direction its low half (the CUDA path's store with collision code 4)."""
+    q = g.shape[0]
+    flat = np.asarray(g, dtype=np.float32).reshape(q, -1)
+    seed = sr_seed(np.arange(flat.shape[1], dtype=np.uint64), timestep)
+    rnd = sr_round_f16 if store.kind == "f16s" else sr_round_bf16
+    out = np.empty(flat.shape, dtype=np.uint16)
+    for l in range(0, q, 2):
+        r = sr_bits(seed, l // 2)
+        out[l] = rnd(flat[l], r & np.uint32(0xFFFF))
+        if l + 1 < q:
+            out[l + 1] = rnd(flat[l + 1], r >> np.uint32(16))
+    out = out.reshape(g.shape)
+    return out.view(np.float16) if store.kind == "f16s" else out
+
+
+def _step_shifted(lat, store, f0, f1, bc_mask, missing, omega, bcs, recovery, stochastic=False, timestep=0):
     """step() with collision code 3 (shifted or FP32 stores, FP32): every pulled value,
     streaming-step result and collision output is a deviation g.  The
     bounce-back kinds copy deviations (w_l = w_opp(l)), the extrapolation blend
@@ -862,19 +925,20 @@ def _step_shifted(lat, store, f0, f1, bc_mask, missing, omega, bcs, recovery):
                 go[lat.opp[l], sel] = (T(1.0) - cs) * gp[l, sel] + cs * g_aux
             gout[:, m] = go
 
-    f1_new = store.encode_deviation(gout)
+    f1_new = encode_stochastic(store, gout, timestep) if stochastic else store.encode_deviation(gout)
     skip = ids == 255
     if skip.any():
         f1_new[:, skip] = f1[:, skip]
     return _recovered(lat, f0, f1, bc_mask, missing, bcs), f1_new
 
 
-def run(lat, store, f0, f1, bc_mask, missing, omega, bcs, steps, collision="BGK", T=np.float64, recovery="after"):
+def run(lat, store, f0, f1, bc_mask, missing, omega, bcs, steps, collision="BGK", T=np.float64, recovery="after",
+        timestep0=0):
     """``steps`` steps with the caller-side swap of XLB's examples
     (mlups_3d.py:78-80).  Returns (f_0, f_1) after the final swap: f_0 holds the
     newest state."""
-    for _ in range(steps):
-        f0, f1 = step(lat, store, f0, f1, bc_mask, missing, omega, bcs, collision, T, recovery)
+    for k in range(steps):
+        f0, f1 = step(lat, store, f0, f1, bc_mask, missing, omega, bcs, collision, T, recovery, timestep0 + k)
         f0, f1 = f1, f0
     return f0, f1
 

@@ -13,6 +13,8 @@ POLICIES = {
     "f16": ("FP32FP16", "f16", np.float32),
     "f16s": ("FP32FP16S", "f16s", np.float32),
     "bf16s": ("FP32BF16S", "bf16s", np.float32),
+    "f16sr": ("FP32FP16SR", "f16s", np.float32),
+    "bf16sr": ("FP32BF16SR", "bf16s", np.float32),
     "fp64f32": ("FP64FP32", "f32", np.float64),
     "fp64f16": ("FP64FP16", "f16", np.float64),
 }
@@ -116,8 +118,13 @@ class Scenario:
         pname, skind, T = POLICIES[policy]
         self.T = T
         self.omega = omega
-        # shifted FP16/BF16 policies run BGK on the stored deviations (the stepper picks it)
-        self.collision = "BGK_SHIFTED" if (collision == "BGK" and pname in ("FP32FP16S", "FP32BF16S")) else collision
+        # shifted FP16/BF16 policies run BGK on the stored deviations (the stepper picks it),
+        # their SR variants with stochastic rounding of the stores
+        self.collision = collision
+        if collision == "BGK" and pname in ("FP32FP16S", "FP32BF16S"):
+            self.collision = "BGK_SHIFTED"
+        if collision in ("BGK", "BGK_SHIFTED") and pname in ("FP32FP16SR", "FP32BF16SR"):
+            self.collision = "BGK_SHIFTED_SR"
         self.lat = O.Lattice(lattice)
         self.store = O.Store(skind, self.lat)
         self.shape = tuple(shape)

@@ -93,17 +93,21 @@ def test_c3_reduced_equals_c_oracle(c3r_oracles, policy):
 
 @pytest.mark.gpu
 def test_c3_reduced_fp32_close_to_fp64():
-    """FP32 against FP64 after 1000 steps of the reduced sphere channel (the FP64
-    path equals the oracle bit for bit, above): velocity 1e-4 and density 1e-5
-    relative L2 over the fluid cells, drag and lift (MomentumTransfer on the
-    final state) 1e-3 of the drag."""
+    """FP32 against FP64 after 100 steps of the reduced sphere channel (the FP64
+    path equals the oracle bit for bit, above): velocity 5e-5 and density 5e-6
+    relative L2 over the fluid cells, force (MomentumTransfer on the sphere) 1e-4
+    of the drag.  Measured with the C restatement, which both GPU paths equal:
+    u 1.3e-5, rho 1.0e-6, force 2.1e-5 at 100 steps.  The FP32 and FP64 runs then
+    part quickly in this impulsively started, under-resolved KBC flow (omega
+    1.977): u 1.0e-4 / 2.8e-4 / 9.5e-4 and force 1 % / 2.3 % / 4.1 % at 200 /
+    300 / 500 steps."""
     from xlb_gb300.operator.force import MomentumTransfer
 
     res = {}
     for policy in ("fp64", "fp32"):
         sc = Scenario("D3Q27", C3R_SHAPE, "channel_regularized", policy, "KBC", omega=C3R_OMEGA)
         f_0, f_1, bcm, mm = sc.gpu_fields()
-        f_0, f_1 = sc.stepper.run(f_0, f_1, bcm, mm, sc.omega, 1000)
+        f_0, f_1 = sc.stepper.run(f_0, f_1, bcm, mm, sc.omega, 100)
         force = MomentumTransfer(sc.xbcs[3])(f_0, f_1, bcm, mm)
         rho, u = _rho_u(sc.lat, sc.to_numpy(f_0))
         fluid = sc.bc_mask.reshape(-1) == 0
@@ -114,4 +118,4 @@ def test_c3_reduced_fp32_close_to_fp64():
     err_f = np.max(np.abs(F32 - F64)) / abs(F64[0])
     msg = f"u {err_u:.3e} rho {err_rho:.3e} force {err_f:.3e} (F64 {F64}, F32 {F32})"
     assert np.all(np.isfinite(u32)) and abs(F64[0]) > 0, msg
-    assert err_u < 1e-4 and err_rho < 1e-5 and err_f < 1e-3, msg
+    assert err_u < 5e-5 and err_rho < 5e-6 and err_f < 1e-4, msg

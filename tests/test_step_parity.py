@@ -284,3 +284,43 @@ def test_kbc_fp32_tma_matches_oracle(lattice, shape, layout, kernel):
     _compare(got0, want0, "f_0")
     _compare(got1, want1, "f_1")
     assert _lib.load().xlbg_device_faults(1) == 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kernel", ["auto", "march", "cell", "tma_wide"])
+@pytest.mark.parametrize("policy", ["f16sr", "bf16sr"])
+@pytest.mark.parametrize("lattice,shape,layout", [
+    ("D3Q19", (10, 8, 16), "channel_regularized"),
+    ("D3Q19", (6, 5, 264), "cavity_fullway"),
+    ("D2Q9", (30, 16), "channel_zouhe"),
+    ("D3Q27", (10, 8, 16), "channel_pressure"),
+    ("D3Q19", (12, 10, 9), "cavity_halfway"),
+])
+def test_stochastic_rounding_matches_oracle(lattice, shape, layout, policy, kernel):
+    """FP32FP16SR / FP32BF16SR: BGK on the stored deviations with every store
+    rounded stochastically (cvt.rs, random bits hashed from the cell index and
+    the timestep argument), bit for bit against the oracle's restatement of
+    cvt.rs and of the hash, on every kernel variant."""
+    from xlb_gb300 import _lib
+
+    sel = {"auto": _lib.KERNEL_AUTO, "march": _lib.KERNEL_MARCH, "cell": _lib.KERNEL_CELL,
+           "tma_wide": _lib.KERNEL_TMA_WIDE}[kernel]
+    sc = Scenario(lattice, shape, layout, policy=policy)
+    sc.randomize(seed=17)
+    want0, want1 = sc.oracle_steps(3)
+    with _lib.forced_kernel(sel):
+        got0, got1 = sc.gpu_steps(3)
+    _compare(got0, want0, "f_0")
+    _compare(got1, want1, "f_1")
+    assert _lib.load().xlbg_device_faults(1) == 0
+
+
+@pytest.mark.gpu
+def test_stochastic_rounding_run_uses_the_timesteps():
+    """xlbg_run seeds step k with timestep0 + k, like the per-step loop."""
+    sc = Scenario("D3Q19", (10, 8, 16), "channel_regularized", policy="f16sr")
+    sc.randomize(seed=18)
+    a = sc.gpu_steps(4)
+    b = sc.gpu_steps(4, use_run=True)
+    _compare(b[0], a[0], "run f_0")
+    _compare(b[1], a[1], "run f_1")

@@ -28,7 +28,7 @@ BC_REGULARIZED_VELOCITY = 6
 BC_REGULARIZED_PRESSURE = 7
 BC_EXTRAPOLATION = 8
 
-BGK, KBC, BGK_PAIR, BGK_SHIFTED = 0, 1, 2, 3
+BGK, KBC, BGK_PAIR, BGK_SHIFTED, BGK_SHIFTED_SR = 0, 1, 2, 3, 4
 
 KERNEL_AUTO, KERNEL_MARCH, KERNEL_MARCH_WIDE, KERNEL_CELL, KERNEL_TMA_WIDE = 0, 1, 2, 3, 4
 

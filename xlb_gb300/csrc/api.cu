@@ -59,8 +59,11 @@ static int check_desc(const xlbg_desc* d) {
   if (d->compute == XLBG_COMPUTE_F64 && (d->store == XLBG_STORE_F16S || d->store == XLBG_STORE_BF16S))
     return fail(XLBG_ERR_UNSUPPORTED, "shifted FP16/BF16 storage is defined with FP32 compute only");
   if (d->collision != XLBG_BGK && d->collision != XLBG_KBC && d->collision != XLBG_BGK_PAIR &&
-      d->collision != XLBG_BGK_SHIFTED)
+      d->collision != XLBG_BGK_SHIFTED && d->collision != XLBG_BGK_SHIFTED_SR)
     return fail(XLBG_ERR_ARG, "unknown collision %d", d->collision);
+  if (d->collision == XLBG_BGK_SHIFTED_SR &&
+      !(d->compute == XLBG_COMPUTE_F32 && (d->store == XLBG_STORE_F16S || d->store == XLBG_STORE_BF16S)))
+    return fail(XLBG_ERR_UNSUPPORTED, "stochastic rounding needs FP32 compute with a shifted FP16/BF16 store");
   if (d->collision == XLBG_BGK_SHIFTED &&
       !(d->compute == XLBG_COMPUTE_F32 &&
         (d->store == XLBG_STORE_F16S || d->store == XLBG_STORE_BF16S || d->store == XLBG_STORE_F32)))
@@ -306,6 +309,7 @@ int fill_step_args(const xlbg_desc* d, const void* f0, void* f1, const uint8_t* 
   for (int b = 0; b < d->nbc; ++b) a.bc_code[d->bc[b].id & 0xff] = (uint16_t)(d->bc[b].kind | (b << 8));
   a.force_id = -1;
   a.diag_slots = nullptr;
+  a.timestep = 0;
   return XLBG_OK;
 }
 
@@ -380,9 +384,10 @@ int check_step_args(const xlbg_desc* d, const void* f0, const void* f1, const ui
 
 int one_step(const xlbg_desc* d, void* f0, void* f1, const uint8_t* bc_mask, const uint32_t* miss,
                     const int64_t* rec_cells, int64_t n_rec, void* rec_scratch, double omega, bool diag,
-                    int force_id, double* slots, double* out, cudaStream_t s) {
+                    int force_id, double* slots, double* out, cudaStream_t s, int timestep) {
   StepArgs a;
   fill_step_args(d, f0, f1, bc_mask, miss, omega, a);
+  a.timestep = (unsigned)timestep;
   a.force_id = force_id;
   a.diag_slots = slots;
   if (n_rec > 0) recovery_pass(d, true, f1, rec_cells, miss, rec_scratch, n_rec, s);
@@ -497,17 +502,15 @@ int xlbg_pack_missing(const xlbg_desc* d, const uint8_t* missing_mask, uint32_t*
 int xlbg_step(const xlbg_desc* d, void* f0, void* f1, const uint8_t* bc_mask, const uint32_t* miss,
               const int64_t* rec_cells, int64_t n_rec, void* rec_scratch, double omega, int32_t timestep,
               void* stream) {
-  (void)timestep;
   int e;
   if ((e = check_step_args(d, f0, f1, bc_mask, miss, rec_cells, n_rec, rec_scratch))) return e;
   return one_step(d, f0, f1, bc_mask, miss, rec_cells, n_rec, rec_scratch, omega, false, -1, nullptr, nullptr,
-                  (cudaStream_t)stream);
+                  (cudaStream_t)stream, timestep);
 }
 
 int xlbg_run(const xlbg_desc* d, void* f0, void* f1, const uint8_t* bc_mask, const uint32_t* miss,
              const int64_t* rec_cells, int64_t n_rec, void* rec_scratch, double omega, int32_t timestep0,
              int32_t n_steps, void* stream) {
-  (void)timestep0;
   int e;
   if ((e = check_step_args(d, f0, f1, bc_mask, miss, rec_cells, n_rec, rec_scratch))) return e;
   if (n_steps < 0) return fail(XLBG_ERR_ARG, "n_steps < 0");
@@ -515,7 +518,7 @@ int xlbg_run(const xlbg_desc* d, void* f0, void* f1, const uint8_t* bc_mask, con
   void* b = f1;
   for (int k = 0; k < n_steps; ++k) {
     if ((e = one_step(d, a, b, bc_mask, miss, rec_cells, n_rec, rec_scratch, omega, false, -1, nullptr, nullptr,
-                      (cudaStream_t)stream)))
+                      (cudaStream_t)stream, timestep0 + k)))
       return e;
     void* t = a;
     a = b;
@@ -527,13 +530,12 @@ int xlbg_run(const xlbg_desc* d, void* f0, void* f1, const uint8_t* bc_mask, con
 int xlbg_step_diag(const xlbg_desc* d, void* f0, void* f1, const uint8_t* bc_mask, const uint32_t* miss,
                    const int64_t* rec_cells, int64_t n_rec, void* rec_scratch, double omega, int32_t timestep,
                    int32_t force_id, double* diag_slots, double* diag, void* stream) {
-  (void)timestep;
   int e;
   if ((e = check_step_args(d, f0, f1, bc_mask, miss, rec_cells, n_rec, rec_scratch))) return e;
   if ((e = check_ptr(diag_slots, 8, "diag_slots"))) return e;
   if ((e = check_ptr(diag, 8, "diag"))) return e;
   return one_step(d, f0, f1, bc_mask, miss, rec_cells, n_rec, rec_scratch, omega, true, force_id, diag_slots, diag,
-                  (cudaStream_t)stream);
+                  (cudaStream_t)stream, timestep);
 }
 
 int xlbg_equilibrium(const xlbg_desc* d, const void* rho, const void* u, double rho0, const double* u0, void* f,

@@ -32,7 +32,7 @@ int check_step_args(const xlbg_desc* d, const void* f0, const void* f1, const ui
                     const int64_t* rec_cells, int64_t n_rec, const void* rec_scratch);
 int one_step(const xlbg_desc* d, void* f0, void* f1, const uint8_t* bc_mask, const uint32_t* miss,
              const int64_t* rec_cells, int64_t n_rec, void* rec_scratch, double omega, bool diag, int force_id,
-             double* slots, double* out, cudaStream_t s);
+             double* slots, double* out, cudaStream_t s, int timestep);
 
 // Block partial sums of the diagnostics reduction (zeroed at the start of each call).
 static __device__ __align__(256) double g_noalloc_diag_slots[XLBG_DIAG_SLOTS * 4];
@@ -87,7 +87,6 @@ using namespace xlbg;
 extern "C" int xlbg_step_diag_noalloc(const xlbg_desc* d, void* f0, void* f1, const uint8_t* bc_mask,
                                       const uint32_t* miss, const int64_t* rec_cells, int64_t n_rec, double omega,
                                       int32_t timestep, int32_t force_id, double* diag, void* stream) {
-  (void)timestep;
   NoallocPtrs p;
   int e;
   if ((e = noalloc_pointers(p))) return e;
@@ -106,5 +105,6 @@ extern "C" int xlbg_step_diag_noalloc(const xlbg_desc* d, void* f0, void* f1, co
   // The slots keep the previous call's contents; the reduction needs them zero.
   cudaError_t ce = cudaMemsetAsync(p.slots, 0, sizeof(double) * XLBG_DIAG_SLOTS * 4, s);
   if (ce != cudaSuccess) return fail(XLBG_ERR_CUDA, "clearing the diagnostics slots: %s", cudaGetErrorString(ce));
-  return one_step(d, f0, f1, bc_mask, miss, rec_cells, n_rec, p.rec, omega, true, force_id, p.slots, diag, s);
+  return one_step(d, f0, f1, bc_mask, miss, rec_cells, n_rec, p.rec, omega, true, force_id, p.slots, diag, s,
+                  timestep);
 }

@@ -9,8 +9,11 @@ namespace xlbg {
 
 // Returns 0 on launch, -1 for an unsupported store/compute pair, or the CUDA error.
 // Pick the instantiation of a BGK form (0, 2 or 3) at run time.
-#define XLBG_BGK_FORM(FN, LAT, ...) \
-  (form == 3 ? FN<LAT, 3>(__VA_ARGS__) : form == 2 ? FN<LAT, 2>(__VA_ARGS__) : FN<LAT, 0>(__VA_ARGS__))
+#define XLBG_BGK_FORM(FN, LAT, ...)                                                                  \
+  (form == 4   ? FN<LAT, 4>(__VA_ARGS__)                                                                \
+   : form == 3 ? FN<LAT, 3>(__VA_ARGS__)                                                                \
+   : form == 2 ? FN<LAT, 2>(__VA_ARGS__)                                                                \
+               : FN<LAT, 0>(__VA_ARGS__))
 template <int LAT, int COLL>
 int launch_step_t(const StepArgs& a, int sk, int compute, bool fullbc, bool diag, cudaStream_t s) {
   using L = Lattice<LAT>;
@@ -24,7 +27,14 @@ int launch_step_t(const StepArgs& a, int sk, int compute, bool fullbc, bool diag
     else                                                                             \
       step_kernel<L, SKV, TV, COLL, false, false><<<grid, kStepBlock, 0, s>>>(a);   \
   } while (0)
-  if constexpr (COLL == 3) {  // deviations: shifted stores or FP32, FP32 compute only
+  if constexpr (COLL == 4) {  // stochastic rounding: shifted 16-bit stores, FP32 compute only
+    if (compute == 1) return -1;
+    switch (sk) {
+      case SK_F16S: XLBG_LAUNCH(SK_F16S, float); break;
+      case SK_BF16S: XLBG_LAUNCH(SK_BF16S, float); break;
+      default: return -1;
+    }
+  } else if constexpr (COLL == 3) {  // deviations: shifted stores or FP32, FP32 compute only
     if (compute == 1) return -1;
     switch (sk) {
       case SK_F32: XLBG_LAUNCH(SK_F32, float); break;
@@ -80,7 +90,14 @@ int launch_step_march_t(const StepArgs& a, int sk, int compute, bool fullbc, int
   const int zblocks = (a.n2 + threads - 1) / threads;
   const dim3 grid((unsigned)(a.n0 * zblocks), (unsigned)((a.n1 + chunk - 1) / chunk));
 #define XLBG_MLAUNCH(SKV, TV) launch_march_variant<L, SKV, TV, COLL>(a, fullbc, grid, threads, chunk, s)
-  if constexpr (COLL == 3) {  // deviations: shifted stores or FP32, FP32 compute only
+  if constexpr (COLL == 4) {  // stochastic rounding: shifted 16-bit stores, FP32 compute only
+    if (compute == 1) return -1;
+    switch (sk) {
+      case SK_F16S: XLBG_MLAUNCH(SK_F16S, float); break;
+      case SK_BF16S: XLBG_MLAUNCH(SK_BF16S, float); break;
+      default: return -1;
+    }
+  } else if constexpr (COLL == 3) {  // deviations: shifted stores or FP32, FP32 compute only
     if (compute == 1) return -1;
     switch (sk) {
       case SK_F32: XLBG_MLAUNCH(SK_F32, float); break;

@@ -59,6 +59,7 @@ struct StepArgs {
   uint16_t bc_code[256];
   int force_id;
   double* diag_slots;  // kDiagSlots x 4 doubles, zero on entry
+  unsigned timestep;   // the step's timestep argument (seeds the stochastic rounding of code 4)
 };
 
 // Element (l, i) of f0 / f1 in the store type.  Idx is the index type of the
@@ -136,10 +137,11 @@ __device__ __forceinline__ void pull_cell(const StepArgs& a, int i0, int i1, int
 }
 
 // Collision of one cell: XLB-order BGK (COLL 0), KBC (COLL 1), pair-form BGK
-// (COLL 2) or BGK on the stored deviations of the shifted stores (COLL 3).
+// (COLL 2) or BGK on deviations (COLL 3; COLL 4 the same with stochastic rounding
+// of the stores).
 template <class L, int SK, class T, int COLL>
 __device__ __forceinline__ void collide(const T (&f)[L::Q], T omega, T (&fo)[L::Q]) {
-  if constexpr (COLL == 3) {
+  if constexpr (COLL >= 3) {
     bgk_shifted<L, SK>(f, omega, fo);
   } else if constexpr (COLL == 2) {
     bgk_pair<L>(f, omega, fo);
@@ -169,6 +171,23 @@ __device__ __forceinline__ void store_cell(const StepArgs& a, Idx cell, const T 
   // plane-and-cell offset per store (3 % faster for FP32)
   Bits* __restrict__ row1 = static_cast<Bits*>(a.f1) + cell;
   const size_t plane = (size_t)a.ncell;
+  if constexpr (COLL == 4) {
+    // stochastic rounding, directions in pairs (the last one alone when Q is odd)
+    const uint32_t seed = sr_seed((uint32_t)cell, a.timestep);
+#pragma unroll
+    for (int l = 0; l < L::Q; l += 2) {
+      const uint32_t p = sr_pack<SK>(fo[l], l + 1 < L::Q ? fo[l + 1] : 0.0f, sr_bits(seed, l / 2));
+      row1[(size_t)l * plane] = (Bits)(p & 0xffffu);
+      if (l + 1 < L::Q) row1[(size_t)(l + 1) * plane] = (Bits)(p >> 16);
+      if constexpr (DIAG) {
+        const T v = St::dec((Bits)(p & 0xffffu), T(weight<L>(l)));
+        msum = l == 0 ? v : msum + v;
+        if (l + 1 < L::Q) msum = msum + St::dec((Bits)(p >> 16), T(weight<L>(l + 1)));
+      }
+    }
+    if constexpr (DIAG) dmass = (double)msum;
+    return;
+  }
 #pragma unroll
   for (int l = 0; l < L::Q; ++l) {
     const Bits b = store_pop<SK, T, COLL>(fo[l], T(weight<L>(l)));
@@ -195,6 +214,22 @@ __device__ __forceinline__ void store_cell_u32(const StepArgs& a, unsigned cell,
   using Bits = typename St::Bits;
   T msum = T(0);
   const size_t plane = (size_t)a.ncell;
+  if constexpr (COLL == 4) {
+    const uint32_t seed = sr_seed(cell, a.timestep);
+#pragma unroll
+    for (int l = 0; l < L::Q; l += 2) {
+      const uint32_t p = sr_pack<SK>(fo[l], l + 1 < L::Q ? fo[l + 1] : 0.0f, sr_bits(seed, l / 2));
+      (static_cast<Bits*>(a.f1) + (size_t)l * plane)[cell] = (Bits)(p & 0xffffu);
+      if (l + 1 < L::Q) (static_cast<Bits*>(a.f1) + (size_t)(l + 1) * plane)[cell] = (Bits)(p >> 16);
+      if constexpr (DIAG) {
+        const T v = St::dec((Bits)(p & 0xffffu), T(weight<L>(l)));
+        msum = l == 0 ? v : msum + v;
+        if (l + 1 < L::Q) msum = msum + St::dec((Bits)(p >> 16), T(weight<L>(l + 1)));
+      }
+    }
+    if constexpr (DIAG) dmass = (double)msum;
+    return;
+  }
 #pragma unroll
   for (int l = 0; l < L::Q; ++l) {
     const Bits b = store_pop<SK, T, COLL>(fo[l], T(weight<L>(l)));
@@ -249,14 +284,14 @@ __device__ __forceinline__ void cell_update(const StepArgs& a, int i0, int i1, i
       T u[L::D];
 #pragma unroll
       for (int d = 0; d < L::D; ++d) u[d] = T(a.bc[slot].u[d]);
-      if constexpr (COLL == 3)
+      if constexpr (COLL >= 3)
         equilibrium_dev<L, SK>((float)(a.bc[slot].rho - 1.0), u, f);
       else
         equilibrium<L>(T(a.bc[slot].rho), u, f);
     } else if (FULLBC && kind >= BC_ZOUHE_V && kind <= BC_REG_P) {
       // the prescribed value lives in slot 0 of f1 (boundary_condition.py:151-152)
       const T aux = St::dec_raw(static_cast<const Bits*>(a.aux)[cell]);
-      if constexpr (COLL == 3)
+      if constexpr (COLL >= 3)
         zouhe_like_dev<L, SK>(f, miss, aux, kind);
       else
         zouhe_like<L>(f, miss, aux, kind);

@@ -261,9 +261,11 @@ __global__ void __launch_bounds__(tma_consumers<PITCH>() + 32,
     }
     __syncwarp();
     if (lane == 0) mbar_arrive(empty + 8 * s);
-    if (__all_sync(0xffffffffu, id == 0)) {
+    if (COLL != 1 && __all_sync(0xffffffffu, id == 0)) {
       // every cell of the warp is fluid (lanes past the row carry id 255): the
       // collision and the store alone, which is what cell_update does for id 0
+      // (BGK forms only: a second inlined copy of the large KBC collision
+      // measured slower)
       T fo[Q];
       collide<L, SK, T, COLL>(f, omega_of<T>(a), fo);
       double dmc = 0.0;
@@ -358,14 +360,16 @@ int launch_tma_t(const CUtensorMap& map, const StepArgs& a, bool fullbc, int row
 }
 
 // Per-lattice entry points (step_tma_*.cu): raw FP16 with XLB-order BGK (code 0),
-// shifted FP16 / BF16 with BGK on the stored deviations (code 3); other
-// combinations return -1.
+// shifted FP16 / BF16 with BGK on the stored deviations (code 3, and code 4 with
+// stochastic rounding); other combinations return -1.
 template <int LAT>
 int launch_tma_lattice(const CUtensorMap& map, const StepArgs& a, int sk, int coll, bool fullbc, int rows, int box,
                        int* err, cudaStream_t s) {
   if (sk == SK_F16 && coll == 0) return launch_tma_t<LAT, SK_F16, 0>(map, a, fullbc, rows, box, err, s);
   if (sk == SK_F16S && coll == 3) return launch_tma_t<LAT, SK_F16S, 3>(map, a, fullbc, rows, box, err, s);
   if (sk == SK_BF16S && coll == 3) return launch_tma_t<LAT, SK_BF16S, 3>(map, a, fullbc, rows, box, err, s);
+  if (sk == SK_F16S && coll == 4) return launch_tma_t<LAT, SK_F16S, 4>(map, a, fullbc, rows, box, err, s);
+  if (sk == SK_BF16S && coll == 4) return launch_tma_t<LAT, SK_BF16S, 4>(map, a, fullbc, rows, box, err, s);
   return -1;
 }
 

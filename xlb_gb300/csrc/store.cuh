@@ -105,19 +105,54 @@ struct Store<SK_BF16S, float> {
 // stored deviation g for code 3.
 template <int SK, class T, int COLL>
 __device__ __forceinline__ T load_pop(typename Store<SK, T>::Bits b, T w) {
-  if constexpr (COLL == 3)
+  if constexpr (COLL >= 3)
     return Store<SK, T>::dev(b, w);
   else
     return Store<SK, T>::dec(b, w);
 }
 
-// The stored bits of a post-collision population (f for codes 0-2, g for code 3).
+// The stored bits of a post-collision population (f for codes 0-2, g for codes
+// 3 and 4; code 4 stores through sr_pack instead, in pairs).
 template <int SK, class T, int COLL>
 __device__ __forceinline__ typename Store<SK, T>::Bits store_pop(T v, T w) {
-  if constexpr (COLL == 3)
+  if constexpr (COLL >= 3)
     return Store<SK, T>::enc_dev(v, w);
   else
     return Store<SK, T>::enc(v, w);
+}
+
+// Stochastic rounding of two FP32 values into a packed pair of the 16-bit store
+// (collision code 4), Blackwell's cvt.rs: `hi` goes to the upper half with
+// random bits rbits[31:16], `lo` to the lower half with rbits[15:0].  FP16: the
+// result is floor(|x| / ulp + r13 / 2^13) ulp with r13 the low 13 of the 16 bits
+// and ulp the FP16 ulp of |x|'s binade (2^-24 below 2^-14); +-inf from 65536 up.
+// BF16: the 16 bits are added to the low half of x's FP32 pattern, which is then
+// truncated.  (Both pinned bit for bit on 10^6 random pairs with random bits.)
+template <int SK>
+__device__ __forceinline__ uint32_t sr_pack(float lo, float hi, uint32_t rbits) {
+  uint32_t d;
+  if constexpr (SK == SK_F16S)
+    asm("cvt.rs.f16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(hi), "f"(lo), "r"(rbits));
+  else
+    asm("cvt.rs.bf16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(hi), "f"(lo), "r"(rbits));
+  return d;
+}
+
+// Random bits of one cell's stochastic rounding: C. Wellons' "lowbias32" integer
+// hash of (cell, timestep), then one multiply by an odd constant per pair k of
+// directions (the rounding needs bits independent of the values, uniform per
+// value, fresh every step; runs stay reproducible).
+__device__ __forceinline__ uint32_t sr_seed(uint32_t cell, uint32_t t) {
+  uint32_t x = cell * 0x9E3779B1u + t * 0x85EBCA77u;
+  x ^= x >> 16;
+  x *= 0x7FEB352Du;
+  x ^= x >> 15;
+  x *= 0x846CA68Bu;
+  x ^= x >> 16;
+  return x;
+}
+__device__ __forceinline__ uint32_t sr_bits(uint32_t seed, int k) {
+  return seed * ((2u * (uint32_t)k + 1u) * 0x9E3779B9u);
 }
 
 template <class Bits>

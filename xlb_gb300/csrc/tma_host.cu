@@ -69,7 +69,8 @@ int try_launch_tma(const xlbg_desc* d, const StepArgs& a, bool fullbc, bool diag
   const int sk = d->store;
   const int coll = d->collision;
   const bool h16 =
-      (sk == SK_F16 && coll == XLBG_BGK) || ((sk == SK_F16S || sk == SK_BF16S) && coll == XLBG_BGK_SHIFTED);
+      (sk == SK_F16 && coll == XLBG_BGK) ||
+      ((sk == SK_F16S || sk == SK_BF16S) && (coll == XLBG_BGK_SHIFTED || coll == XLBG_BGK_SHIFTED_SR));
   // FP32 D3Q27 KBC: the compute-heavy sphere-channel step, also with diagnostics
   const bool kbc32 = sk == SK_F32 && coll == XLBG_KBC && d->lattice == XLBG_D3Q27;
   if (!(h16 && !diag) && !kbc32) return 1;

@@ -59,17 +59,23 @@ class IncompressibleNavierStokesStepper(Stepper):
         super().__init__(grid, boundary_conditions)
         if collision_type == "BGK":
             # The shifted FP16/BF16 forms have no XLB counterpart and run BGK on the
-            # stored deviations (same equations, pair form); the others keep XLB's order.
-            self.collision_code = _lib.BGK_SHIFTED if self.precision_policy.shifted else _lib.BGK
+            # stored deviations (same equations, pair form; their SR variants round
+            # the stores stochastically); the others keep XLB's order.
+            pp = self.precision_policy
+            self.collision_code = (_lib.BGK_SHIFTED_SR if pp.stochastic else _lib.BGK_SHIFTED) if pp.shifted else _lib.BGK
         elif collision_type == "BGK_SHIFTED":
             pp = self.precision_policy
             if not (pp.shifted or (pp.store_code, pp.compute_code) == (0, 0)):
                 raise ValueError("BGK_SHIFTED needs FP32 compute with a shifted or FP32 store "
                                  "(FP32FP16S, FP32BF16S, FP32FP32)")
-            self.collision_code = _lib.BGK_SHIFTED
+            self.collision_code = _lib.BGK_SHIFTED_SR if pp.stochastic else _lib.BGK_SHIFTED
         elif collision_type == "BGK_PAIR":
+            if self.precision_policy.stochastic:
+                raise ValueError("stochastic rounding is defined for BGK on the stored deviations only")
             self.collision_code = _lib.BGK_PAIR
         elif collision_type == "KBC":
+            if self.precision_policy.stochastic:
+                raise ValueError("stochastic rounding is defined for BGK on the stored deviations only")
             if (self.velocity_set.d, self.velocity_set.q) == (3, 19):
                 raise NotImplementedError(f"Velocity set not supported for KBC: {self.velocity_set}")
             self.collision_code = _lib.KBC

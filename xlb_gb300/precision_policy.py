@@ -8,6 +8,11 @@ the same member names).  Two store forms are new here:
   Rev. E 106, 015308 (2022); the power-of-two scale keeps small deviations out of
   FP16's subnormal range).  XLB's ``FP32FP16`` stores raw FP16 and is kept as-is.
 * ``FP32BF16S`` -- f_l - w_l in BF16 (no scale: BF16 has FP32's exponent range).
+* ``FP32FP16SR`` / ``FP32BF16SR`` -- the same stored values, rounded
+  stochastically on store (Blackwell's ``cvt.rs`` with hashed random bits of
+  the cell and time step) instead of to nearest: a per-step change smaller than
+  half a 16-bit ulp then survives in expectation instead of being lost in every
+  cell that sits near a steady value.
 
 With shifted storage every population slot holds the (scaled) ``f - w_l``,
 except the boundary auxiliary value that ZouHe / Regularized keep in slot 0 of
@@ -70,6 +75,8 @@ class PrecisionPolicy(Enum):
     FP32FP16 = auto()
     FP32FP16S = auto()
     FP32BF16S = auto()
+    FP32FP16SR = auto()
+    FP32BF16SR = auto()
 
     @property
     def compute_precision(self):
@@ -87,18 +94,26 @@ class PrecisionPolicy(Enum):
             PrecisionPolicy.FP32FP16: Precision.FP16,
             PrecisionPolicy.FP32FP16S: Precision.FP16,
             PrecisionPolicy.FP32BF16S: Precision.BF16,
+            PrecisionPolicy.FP32FP16SR: Precision.FP16,
+            PrecisionPolicy.FP32BF16SR: Precision.BF16,
         }[self]
 
     @property
     def shifted(self):
         """True when populations are stored as f - w_l."""
-        return self in (PrecisionPolicy.FP32FP16S, PrecisionPolicy.FP32BF16S)
+        return self in (PrecisionPolicy.FP32FP16S, PrecisionPolicy.FP32BF16S, PrecisionPolicy.FP32FP16SR,
+                        PrecisionPolicy.FP32BF16SR)
+
+    @property
+    def stochastic(self):
+        """True when stores round stochastically (the shifted forms' SR variants)."""
+        return self in (PrecisionPolicy.FP32FP16SR, PrecisionPolicy.FP32BF16SR)
 
     @property
     def store_code(self):
-        if self == PrecisionPolicy.FP32FP16S:
+        if self in (PrecisionPolicy.FP32FP16S, PrecisionPolicy.FP32FP16SR):
             return STORE_F16S
-        if self == PrecisionPolicy.FP32BF16S:
+        if self in (PrecisionPolicy.FP32BF16S, PrecisionPolicy.FP32BF16SR):
             return STORE_BF16S
         return {Precision.FP32: STORE_F32, Precision.FP64: STORE_F64, Precision.FP16: STORE_F16}[self.store_precision]
 
