@@ -109,7 +109,10 @@ __device__ __forceinline__ void kbc(const T (&f)[L::Q], const T (&feq)[L::Q], T 
 #pragma unroll
   for (int l = 0; l < L::Q; ++l) {
     dh[l] = fneq[l] - ds[l];
-    const T temp = dh[l] / feq[l];
+    // dh / feq, with feq > 0: a zero dh (cells still at their initial equilibrium)
+    // is its own quotient, sign included, and skips the division's slow path,
+    // which every zero dividend took
+    const T temp = dh[l] == T(0) ? dh[l] : dh[l] / feq[l];
     sp1 = sp1 + temp * ds[l];
     sp2 = sp2 + temp * dh[l];
   }

@@ -1,6 +1,6 @@
 // TMA-staged step kernels for D3Q19 with the 16-bit stores (one lattice per
 // translation unit so the build parallelises).
-#include "step_tma.cuh"
+#include "step_tma_pair.cuh"
 
 namespace xlbg {
 int launch_step_tma_d3q19(const CUtensorMap& map, const StepArgs& a, int sk, int coll, bool fullbc, int rows, int box,
