@@ -360,10 +360,9 @@ int launch_tma_t(const CUtensorMap& map, const StepArgs& a, bool fullbc, int row
 }
 
 // Per-lattice entry points (step_tma_*.cu): raw FP16 with XLB-order BGK (code 0),
-// shifted FP16 / BF16 with BGK on the stored deviations (code 3 on the two-cell
-// kernel of step_tma_pair.cuh, code 4 with stochastic rounding on this one);
-// other combinations return -1.
-template <int LAT, int SK>
+// shifted FP16 / BF16 with BGK on the stored deviations (codes 3 and 4, on the
+// two-cell kernel of step_tma_pair.cuh); other combinations return -1.
+template <int LAT, int SK, int COLL>
 int launch_tma_pair_t(const CUtensorMap& map, const StepArgs& a, bool fullbc, int rows, int box, int* err,
                       cudaStream_t s);
 
@@ -371,10 +370,10 @@ template <int LAT>
 int launch_tma_lattice(const CUtensorMap& map, const StepArgs& a, int sk, int coll, bool fullbc, int rows, int box,
                        int* err, cudaStream_t s) {
   if (sk == SK_F16 && coll == 0) return launch_tma_t<LAT, SK_F16, 0>(map, a, fullbc, rows, box, err, s);
-  if (sk == SK_F16S && coll == 3) return launch_tma_pair_t<LAT, SK_F16S>(map, a, fullbc, rows, box, err, s);
-  if (sk == SK_BF16S && coll == 3) return launch_tma_pair_t<LAT, SK_BF16S>(map, a, fullbc, rows, box, err, s);
-  if (sk == SK_F16S && coll == 4) return launch_tma_t<LAT, SK_F16S, 4>(map, a, fullbc, rows, box, err, s);
-  if (sk == SK_BF16S && coll == 4) return launch_tma_t<LAT, SK_BF16S, 4>(map, a, fullbc, rows, box, err, s);
+  if (sk == SK_F16S && coll == 3) return launch_tma_pair_t<LAT, SK_F16S, 3>(map, a, fullbc, rows, box, err, s);
+  if (sk == SK_BF16S && coll == 3) return launch_tma_pair_t<LAT, SK_BF16S, 3>(map, a, fullbc, rows, box, err, s);
+  if (sk == SK_F16S && coll == 4) return launch_tma_pair_t<LAT, SK_F16S, 4>(map, a, fullbc, rows, box, err, s);
+  if (sk == SK_BF16S && coll == 4) return launch_tma_pair_t<LAT, SK_BF16S, 4>(map, a, fullbc, rows, box, err, s);
   return -1;
 }
 

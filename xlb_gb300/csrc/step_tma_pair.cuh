@@ -1,5 +1,6 @@
 // TMA-staged step with two cells per consumer thread, for BGK on the stored
-// deviations of the shifted 16-bit stores (collision code 3).
+// deviations of the shifted 16-bit stores (collision code 3, and code 4 with
+// stochastic rounding).
 //
 // The one-cell consumer of step_kernel_tma spends about 440 instructions a cell
 // (issue-bound at ~75 % of the 77 B/cell roof).  Here thread j owns cells 2j and
@@ -10,7 +11,9 @@
 // rounding (explicit .rn: no contraction), so the results are bit-identical to
 // the one-cell kernel and the oracle.  The two cells' values of a direction
 // convert with one cvt.rn.{f16x2,bf16x2} and store as one 32-bit word (the pair
-// is 4-byte aligned: rows hold a multiple of 8 cells).
+// is 4-byte aligned: rows hold a multiple of 8 cells).  With stochastic rounding
+// (code 4) the conversion is cvt.rs with each half given the 16 random bits the
+// one-cell store gives that (cell, direction), so results stay identical too.
 //
 // Warps whose 64 cells are all fluid take the packed path; any other warp runs
 // cell_update on its two cells one after the other.  The ring, the producer warp
@@ -173,7 +176,7 @@ __host__ __device__ constexpr int tma2_min_blocks() {
   return PITCH <= 256 ? 4 : (PITCH == 512 ? 2 : 1);
 }
 
-template <class L, int SK, bool FULLBC, int PITCH, bool WIDE>
+template <class L, int SK, int COLL, bool FULLBC, int PITCH, bool WIDE>
 __global__ void __launch_bounds__(tma2_consumers<PITCH>() + 32, tma2_min_blocks<PITCH>())
     step_kernel_tma_pair(const __grid_constant__ CUtensorMap map, const StepArgs a, int rows, int box, int* err) {
   using T = float;
@@ -181,7 +184,7 @@ __global__ void __launch_bounds__(tma2_consumers<PITCH>() + 32, tma2_min_blocks<
   using St = Store<SK, T>;
   using Bits = typename St::Bits;
   static_assert(sizeof(Bits) == 2, "16-bit stores");
-  constexpr int COLL = 3;
+  static_assert(COLL == 3 || COLL == 4, "BGK on deviations");
   constexpr int Q = L::Q;
   constexpr int S = tma_stages<L>();
   constexpr unsigned ROW = PITCH * 2;
@@ -262,10 +265,26 @@ __global__ void __launch_bounds__(tma2_consumers<PITCH>() + 32, tma2_min_blocks<
     if (__all_sync(0xffffffffu, ids == 0)) {
       // 64 fluid cells: the packed collision, one 32-bit store per direction
       bgk_shifted2<L, SK>(g, omega_of<T>(a));
+      if constexpr (COLL == 4) {
+        // the one-cell store rounds (cell c, direction l) with the low (l even) or
+        // high (l odd) 16 bits of sr_bits(sr_seed(c, t), l / 2): assemble those
+        // of cells c0 (low half) and c0 + 1 (high half) per direction
+        const uint32_t s0 = sr_seed(cell, a.timestep), s1 = sr_seed(cell + 1u, a.timestep);
 #pragma unroll
-      for (int l = 0; l < Q; ++l) {
-        uint32_t* __restrict__ dst = reinterpret_cast<uint32_t*>(static_cast<Bits*>(a.f1) + (size_t)l * plane + cell);
-        *dst = pack_rn2<SK>(g[l]);
+        for (int l = 0; l < Q; ++l) {
+          const uint32_t w0 = sr_bits(s0, l / 2), w1 = sr_bits(s1, l / 2);
+          const uint32_t rb = (l & 1) ? __byte_perm(w0, w1, 0x7632) : __byte_perm(w0, w1, 0x5410);
+          uint32_t* __restrict__ dst =
+              reinterpret_cast<uint32_t*>(static_cast<Bits*>(a.f1) + (size_t)l * plane + cell);
+          *dst = sr_pack<SK>(lo2(g[l]), hi2(g[l]), rb);
+        }
+      } else {
+#pragma unroll
+        for (int l = 0; l < Q; ++l) {
+          uint32_t* __restrict__ dst =
+              reinterpret_cast<uint32_t*>(static_cast<Bits*>(a.f1) + (size_t)l * plane + cell);
+          *dst = pack_rn2<SK>(g[l]);
+        }
       }
     } else {
       // cell by cell through cell_update (boundary cells, skip cells, row ends)
@@ -283,39 +302,39 @@ __global__ void __launch_bounds__(tma2_consumers<PITCH>() + 32, tma2_min_blocks<
   }
 }
 
-template <class L, int SK, bool FULLBC, int PITCH, bool WIDE>
+template <class L, int SK, int COLL, bool FULLBC, int PITCH, bool WIDE>
 int launch_tma_pair_kernel(const CUtensorMap& map, const StepArgs& a, int rows, int box, int* err, cudaStream_t s) {
   const unsigned smem = tma_smem_bytes<L, 2, PITCH>();
-  static const bool attr = cudaFuncSetAttribute(step_kernel_tma_pair<L, SK, FULLBC, PITCH, WIDE>,
+  static const bool attr = cudaFuncSetAttribute(step_kernel_tma_pair<L, SK, COLL, FULLBC, PITCH, WIDE>,
                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem) == cudaSuccess;
   if (!attr) return (int)cudaErrorInvalidValue;
   const dim3 grid((unsigned)a.n0, (unsigned)((a.n1 + rows - 1) / rows));
-  step_kernel_tma_pair<L, SK, FULLBC, PITCH, WIDE>
+  step_kernel_tma_pair<L, SK, COLL, FULLBC, PITCH, WIDE>
       <<<grid, tma2_consumers<PITCH>() + 32, smem, s>>>(map, a, rows, box, err);
   return (int)cudaGetLastError();
 }
 
-template <class L, int SK, int PITCH>
+template <class L, int SK, int COLL, int PITCH>
 int launch_tma_pair_pitch(const CUtensorMap& map, const StepArgs& a, bool fullbc, int rows, int box, int* err,
                           cudaStream_t s) {
   if (a.wide)
-    return fullbc ? launch_tma_pair_kernel<L, SK, true, PITCH, true>(map, a, rows, box, err, s)
-                  : launch_tma_pair_kernel<L, SK, false, PITCH, true>(map, a, rows, box, err, s);
-  return fullbc ? launch_tma_pair_kernel<L, SK, true, PITCH, false>(map, a, rows, box, err, s)
-                : launch_tma_pair_kernel<L, SK, false, PITCH, false>(map, a, rows, box, err, s);
+    return fullbc ? launch_tma_pair_kernel<L, SK, COLL, true, PITCH, true>(map, a, rows, box, err, s)
+                  : launch_tma_pair_kernel<L, SK, COLL, false, PITCH, true>(map, a, rows, box, err, s);
+  return fullbc ? launch_tma_pair_kernel<L, SK, COLL, true, PITCH, false>(map, a, rows, box, err, s)
+                : launch_tma_pair_kernel<L, SK, COLL, false, PITCH, false>(map, a, rows, box, err, s);
 }
 
-// Shifted 16-bit stores with collision code 3 on the two-cell kernel; staged
-// rows of 256, 512 or 1024 cells (n2 <= 992, so up to 512 consumers).  The host
-// checks that bc_mask is 2-byte and f1 4-byte aligned (ids load in pairs, outputs
-// store in pairs).
-template <int LAT, int SK>
+// Shifted 16-bit stores with collision code 3 or 4 on the two-cell kernel;
+// staged rows of 256, 512 or 1024 cells (n2 <= 992, so up to 496 consumers).
+// The host checks that bc_mask is 2-byte and f1 4-byte aligned (ids load in
+// pairs, outputs store in pairs).
+template <int LAT, int SK, int COLL>
 int launch_tma_pair_t(const CUtensorMap& map, const StepArgs& a, bool fullbc, int rows, int box, int* err,
                       cudaStream_t s) {
   using L = Lattice<LAT>;
-  if (a.n2 <= 256) return launch_tma_pair_pitch<L, SK, 256>(map, a, fullbc, rows, box, err, s);
-  if (a.n2 <= 512) return launch_tma_pair_pitch<L, SK, 512>(map, a, fullbc, rows, box, err, s);
-  return launch_tma_pair_pitch<L, SK, 1024>(map, a, fullbc, rows, box, err, s);
+  if (a.n2 <= 256) return launch_tma_pair_pitch<L, SK, COLL, 256>(map, a, fullbc, rows, box, err, s);
+  if (a.n2 <= 512) return launch_tma_pair_pitch<L, SK, COLL, 512>(map, a, fullbc, rows, box, err, s);
+  return launch_tma_pair_pitch<L, SK, COLL, 1024>(map, a, fullbc, rows, box, err, s);
 }
 
 }  // namespace xlbg

@@ -80,8 +80,8 @@ int try_launch_tma(const xlbg_desc* d, const StepArgs& a, bool fullbc, bool diag
   if (a.n2 < 8 || a.n2 > (kbc32 ? 512 : 992) || (a.n2 * eb) % 16 != 0) return 1;
   if (a.ncell >= 0x7fffffffLL) return 1;
   if (reinterpret_cast<uintptr_t>(a.f0) % 16 != 0) return 1;
-  // the two-cell kernel of collision code 3 loads ids and stores outputs in pairs
-  if (coll == XLBG_BGK_SHIFTED &&
+  // the two-cell kernel of collision codes 3 and 4 loads ids and stores outputs in pairs
+  if ((coll == XLBG_BGK_SHIFTED || coll == XLBG_BGK_SHIFTED_SR) &&
       (reinterpret_cast<uintptr_t>(a.bc_mask) % 2 != 0 || reinterpret_cast<uintptr_t>(a.f1) % 4 != 0))
     return 1;
   EncodeTiledFn enc = encode_fn();
