@@ -41,6 +41,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=100)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--n", type=int, default=512, help="cube edge")
+    p.add_argument("--shape", default=None, help="nx,ny,nz of the cavity instead of a cube (small profiling cases)")
     p.add_argument("--no-forms", action="store_true", help="skip the FP16/BF16 store-form lines")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
@@ -271,16 +272,18 @@ def timed_slabs(ds, slabs, omega, steps, warmup):
     return start.elapsed_time(end)
 
 
-def slabs_on_one_gpu(n, steps, warmup, n_slabs=2):
-    """The n^3 cavity as n_slabs slabs on this GPU: MLUPS of the sharded step."""
+def slabs_on_one_gpu(shape, steps, warmup, n_slabs=2):
+    """The cavity of ``shape`` as n_slabs slabs on this GPU: MLUPS of the sharded step."""
     from xlb_gb300.distribute import DistributedStepper, LocalTransport
 
-    st = cavity_stepper((n, n, n), "FP32FP32")
+    st = cavity_stepper(shape, "FP32FP32")
     ds = DistributedStepper(st, n_slabs=n_slabs, transport=LocalTransport())
     slabs = ds.prepare_fields()
     ms = timed_slabs(ds, slabs, 1.8, steps, warmup)
-    return {"n_slabs": n_slabs, "MLUPS": n**3 * steps / (ms * 1e-3) / 1e6, "ms_per_step": ms / steps,
-            "what": f"{n}^3 FP32 cavity as {n_slabs} x-slabs on one GPU, ghost planes exchanged by device copies"}
+    cells = shape[0] * shape[1] * shape[2]
+    return {"n_slabs": n_slabs, "MLUPS": cells * steps / (ms * 1e-3) / 1e6, "ms_per_step": ms / steps,
+            "what": f"{'x'.join(map(str, shape))} FP32 cavity as {n_slabs} x-slabs on one GPU, ghost planes exchanged "
+                    "by device copies"}
 
 
 def run_sharded(args, world, rank, local):
@@ -314,7 +317,7 @@ def run_sharded(args, world, rank, local):
         },
         "gpu_launches": args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": load_traffic(n), "bytes_per_cell": BYTES_PER_CELL[("D3Q19", 4)],
+                     "traffic": load_traffic(cells), "bytes_per_cell": BYTES_PER_CELL[("D3Q19", 4)],
                      "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})"},
         "clocks": clk.summary(),
     }
@@ -395,10 +398,12 @@ def main():
         _dist.destroy_process_group()
         return
     n = args.n
-    cells = n**3
+    shape = tuple(int(v) for v in args.shape.split(",")) if args.shape else (n, n, n)
+    cells = shape[0] * shape[1] * shape[2]
+    label = "x".join(map(str, shape)) if args.shape else f"{n}^3"
     peak, peak_kind = measured_peaks()
 
-    stepper, fields, omega = cavity_setup(n, "FP32FP32")
+    stepper, fields, omega = cavity_setup(shape, "FP32FP32")
     with ClockSampler(local) as clk:
         ms, fields = timed_device(stepper, fields, omega, args.steps, args.warmup)
     ms = max_over_ranks(ms)
@@ -420,7 +425,7 @@ def main():
         "dtype": "f32",
         "data": "synthetic",
         "config": {
-            "workload": f"D3Q19 BGK lid-driven cavity {n}^3, FP32FP32, FullwayBB x5 faces + EquilibriumBC lid u=(0.05,0,0), omega=1.8",
+            "workload": f"D3Q19 BGK lid-driven cavity {label}, FP32FP32, FullwayBB x5 faces + EquilibriumBC lid u=(0.05,0,0), omega=1.8",
             "cells": cells,
             "l2": "inputs (2 x %.1f GB populations) larger than L2; no flush" % (cells * 19 * 4 / 1e9),
             "parallelism": "single GPU",
@@ -432,7 +437,7 @@ def main():
             "peak": peak,
             "unit": "GB/s",
             "frac": achieved / peak,
-            "traffic": load_traffic(n),
+            "traffic": load_traffic(cells),
             "bytes_per_cell": bpc,
             "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})",
         },
@@ -444,7 +449,7 @@ def main():
         torch.cuda.empty_cache()
         for name, pol in (("fp16_shifted", "FP32FP16S"), ("bf16_shifted", "FP32BF16S"),
                           ("fp16_shifted_sr", "FP32FP16SR"), ("bf16_shifted_sr", "FP32BF16SR")):
-            st, fl, om = cavity_setup(n, pol)
+            st, fl, om = cavity_setup(shape, pol)
             ms2, fl = timed_device(st, fl, om, args.steps, args.warmup)
             ms2 = max_over_ranks(ms2)
             v = world * cells * args.steps / (ms2 * 1e-3) / 1e6
@@ -453,14 +458,14 @@ def main():
             del st, fl
             torch.cuda.empty_cache()
         out["store_forms"] = forms
-        stepper, fields, omega = cavity_setup(n, "FP32FP32")
+        stepper, fields, omega = cavity_setup(shape, "FP32FP32")
     if not args.no_slabs:
         del fields, stepper
         torch.cuda.empty_cache()
-        out["slabs_one_gpu"] = slabs_on_one_gpu(n, args.steps, args.warmup)
+        out["slabs_one_gpu"] = slabs_on_one_gpu(shape, args.steps, args.warmup)
         out["slabs_one_gpu"]["x_single_domain"] = out["slabs_one_gpu"]["MLUPS"] / mlups
         torch.cuda.empty_cache()
-        stepper, fields, omega = cavity_setup(n, "FP32FP32")
+        stepper, fields, omega = cavity_setup(shape, "FP32FP32")
     if not args.no_e2e:
         dt, h2d, d2h = timed_e2e(stepper, fields, omega, args.steps)
         dt = max_over_ranks(dt)
@@ -485,7 +490,7 @@ def main():
         _dist.destroy_process_group()
 
 
-def load_traffic(n):
+def load_traffic(cells):
     """dram bytes per launch from the committed ncu summary of this kernel, when present."""
     path = os.path.join(ROOT, "profiles", "step_d3q19_cavity_traffic.json")
     if not os.path.exists(path):
@@ -493,7 +498,7 @@ def load_traffic(n):
     with open(path) as fh:
         d = json.load(fh)
     # traffic grows with the cell count; scale from the captured case
-    return d["dram_bytes_per_launch"] * (n**3) / d["cells"]
+    return d["dram_bytes_per_launch"] * cells / d["cells"]
 
 
 if __name__ == "__main__":
