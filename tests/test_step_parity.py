@@ -176,7 +176,7 @@ TMA_CASES = [
     ("D3Q19", (10, 8, 16), "channel_zouhe"),
     ("D3Q19", (10, 8, 16), "channel_regularized"),
     ("D3Q19", (6, 5, 264), "cavity_fullway"),  # two tensor copies per row, the second partly outside
-    ("D3Q19", (4, 3, 520), "periodic"),  # 1024-thread blocks, three copies per row
+    ("D3Q19", (4, 3, 520), "periodic"),  # shifted stores: three segments; raw FP16: 1024-thread blocks
     ("D2Q9", (30, 24), "channel_regularized"),
     ("D3Q27", (10, 8, 16), "channel_pressure"),
     ("D3Q27", (6, 5, 256), "cavity_halfway"),
@@ -196,6 +196,44 @@ def test_tma_staged_step_matches_oracle(lattice, shape, layout, policy):
         sc.bc_mask[0, 0, 1:3, 201:206] = 255  # odd bounds: cell pairs with one skip cell
     want0, want1 = sc.oracle_steps(3)
     got0, got1 = sc.gpu_steps(3)
+    _compare(got0, want0, "f_0")
+    _compare(got1, want1, "f_1")
+    assert _lib.load().xlbg_device_faults(1) == 0
+
+
+SEG_CASES = [
+    # segments of 256 cells of the contiguous axis
+    ("D3Q19", (10, 8, 16), "channel_zouhe"),  # one segment: both aprons wrap
+    ("D3Q19", (10, 8, 16), "channel_regularized"),
+    ("D3Q19", (6, 5, 264), "cavity_fullway"),  # segments of 256 and 8
+    ("D3Q19", (4, 3, 520), "periodic"),  # 256, 256, 8; skip cells across segment ends
+    ("D3Q19", (3, 4, 1032), "periodic"),  # longer than any full-row stage
+    ("D2Q9", (30, 24), "channel_regularized"),
+    ("D2Q9", (12, 528), "cavity_fullway"),
+    ("D3Q27", (10, 8, 16), "channel_pressure"),
+    ("D3Q27", (4, 3, 768), "cavity_halfway"),
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kernel", ["auto", "tma_wide"])
+@pytest.mark.parametrize("policy", ["f16s", "bf16s", "f16sr", "bf16sr"])
+@pytest.mark.parametrize("lattice,shape,layout", SEG_CASES)
+def test_segmented_step_matches_oracle(lattice, shape, layout, policy, kernel):
+    """The segmented two-cell kernel of the shifted stores (rows staged as
+    256-cell segments with 16-byte aprons), with 32- and 64-bit plane offsets,
+    bit for bit against the oracle."""
+    from xlb_gb300 import _lib
+
+    sel = _lib.KERNEL_AUTO if kernel == "auto" else _lib.KERNEL_TMA_WIDE
+    sc = Scenario(lattice, shape, layout, policy=policy)
+    sc.randomize(seed=19)
+    if layout == "periodic":
+        sc.bc_mask[0, 1:3, 0:2, 250:262] = 255  # skip cells across the first segment end
+        sc.bc_mask[0, 0, 1:3, 509:514] = 255  # odd bounds: cell pairs with one skip cell
+    want0, want1 = sc.oracle_steps(3)
+    with _lib.forced_kernel(sel):
+        got0, got1 = sc.gpu_steps(3)
     _compare(got0, want0, "f_0")
     _compare(got1, want1, "f_1")
     assert _lib.load().xlbg_device_faults(1) == 0

@@ -1,0 +1,10 @@
+// Segmented two-cell step kernels for D2Q9 with the shifted 16-bit stores
+// (one lattice per translation unit so the build parallelises).
+#include "step_tma_seg.cuh"
+
+namespace xlbg {
+int launch_step_seg_d2q9(const StepArgs& a, int sk, int coll, bool fullbc, int nseg, int rows, int* err,
+                         cudaStream_t s) {
+  return launch_seg_lattice<0>(a, sk, coll, fullbc, nseg, rows, err, s);
+}
+}  // namespace xlbg

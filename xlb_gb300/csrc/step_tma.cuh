@@ -359,21 +359,13 @@ int launch_tma_t(const CUtensorMap& map, const StepArgs& a, bool fullbc, int row
   }
 }
 
-// Per-lattice entry points (step_tma_*.cu): raw FP16 with XLB-order BGK (code 0),
-// shifted FP16 / BF16 with BGK on the stored deviations (codes 3 and 4, on the
-// two-cell kernel of step_tma_pair.cuh); other combinations return -1.
-template <int LAT, int SK, int COLL>
-int launch_tma_pair_t(const CUtensorMap& map, const StepArgs& a, bool fullbc, int rows, int box, int* err,
-                      cudaStream_t s);
-
+// Per-lattice entry points (step_tma_*.cu): raw FP16 with XLB-order BGK (code
+// 0); other combinations return -1 (the shifted stores take the segmented
+// kernel of step_tma_seg.cuh).
 template <int LAT>
 int launch_tma_lattice(const CUtensorMap& map, const StepArgs& a, int sk, int coll, bool fullbc, int rows, int box,
                        int* err, cudaStream_t s) {
   if (sk == SK_F16 && coll == 0) return launch_tma_t<LAT, SK_F16, 0>(map, a, fullbc, rows, box, err, s);
-  if (sk == SK_F16S && coll == 3) return launch_tma_pair_t<LAT, SK_F16S, 3>(map, a, fullbc, rows, box, err, s);
-  if (sk == SK_BF16S && coll == 3) return launch_tma_pair_t<LAT, SK_BF16S, 3>(map, a, fullbc, rows, box, err, s);
-  if (sk == SK_F16S && coll == 4) return launch_tma_pair_t<LAT, SK_F16S, 4>(map, a, fullbc, rows, box, err, s);
-  if (sk == SK_BF16S && coll == 4) return launch_tma_pair_t<LAT, SK_BF16S, 4>(map, a, fullbc, rows, box, err, s);
   return -1;
 }
 
@@ -383,6 +375,15 @@ int launch_step_tma_d3q19(const CUtensorMap& map, const StepArgs& a, int sk, int
                           int box, int* err, cudaStream_t s);
 int launch_step_tma_d3q27(const CUtensorMap& map, const StepArgs& a, int sk, int coll, bool fullbc, int rows,
                           int box, int* err, cudaStream_t s);
+// Segmented two-cell kernel (step_tma_seg.cuh): shifted 16-bit stores, codes 3
+// and 4; blocks own kSeg cells of the contiguous axis.
+constexpr int kSeg = 256;
+int launch_step_seg_d2q9(const StepArgs& a, int sk, int coll, bool fullbc, int nseg, int rows, int* err,
+                         cudaStream_t s);
+int launch_step_seg_d3q19(const StepArgs& a, int sk, int coll, bool fullbc, int nseg, int rows, int* err,
+                          cudaStream_t s);
+int launch_step_seg_d3q27(const StepArgs& a, int sk, int coll, bool fullbc, int nseg, int rows, int* err,
+                          cudaStream_t s);
 // FP32 store, KBC, D3Q27, with the diagnostics step (step_tma_d3q27_kbc.cu).
 int launch_step_tma_d3q27_kbc32(const CUtensorMap& map, const StepArgs& a, bool fullbc, int rows, int box, int* err,
                                 cudaStream_t s);

@@ -1,6 +1,6 @@
-// TMA-staged step kernels for D3Q27 with the 16-bit stores (one lattice per
+// TMA-staged step kernels for D3Q27 with raw FP16 stores (one lattice per
 // translation unit so the build parallelises).
-#include "step_tma_pair.cuh"
+#include "step_tma.cuh"
 
 namespace xlbg {
 int launch_step_tma_d3q27(const CUtensorMap& map, const StepArgs& a, int sk, int coll, bool fullbc, int rows, int box,

@@ -58,35 +58,61 @@ int* fault_ptr() {
 }  // namespace
 
 // Launches the TMA-staged step when it applies: a 16-bit store with FP32
-// compute (raw FP16 with XLB-order BGK, FP16/BF16 shifted with BGK on the
-// stored deviations), no diagnostics, a contiguous axis of 8..992 cells that is
-// a multiple of 8, fewer than 2^31 cells and a 16-byte aligned f0.  Boundary
-// paths index planes in 32 bits when Q * cells < 2^32, else in 64 bits (as do
-// the calls made with a.wide set).  Returns 1 when it does not apply (the caller
-// uses the marching kernel), else the status.
+// compute, no diagnostics, a contiguous axis of at least 8 cells that is a
+// multiple of 8, fewer than 2^31 cells and a 16-byte aligned f0.  The shifted
+// stores with BGK on their deviations (codes 3 and 4) take the segmented
+// two-cell kernel (any row length); raw FP16 with XLB-order BGK stages whole
+// rows of at most 992 cells, and FP32 D3Q27 KBC (also with diagnostics) whole
+// rows of at most 512.  Boundary paths index planes in 32 bits when Q * cells <
+// 2^32, else in 64 bits (as do the calls made with a.wide set).  Returns 1 when
+// it does not apply (the caller uses the marching kernel), else the status.
 int try_launch_tma(const xlbg_desc* d, const StepArgs& a, bool fullbc, bool diag, cudaStream_t s) {
   if (d->compute != XLBG_COMPUTE_F32) return 1;
   const int sk = d->store;
   const int coll = d->collision;
-  const bool h16 =
-      (sk == SK_F16 && coll == XLBG_BGK) ||
-      ((sk == SK_F16S || sk == SK_BF16S) && (coll == XLBG_BGK_SHIFTED || coll == XLBG_BGK_SHIFTED_SR));
+  const bool pair = (sk == SK_F16S || sk == SK_BF16S) && (coll == XLBG_BGK_SHIFTED || coll == XLBG_BGK_SHIFTED_SR);
+  const bool h16 = (sk == SK_F16 && coll == XLBG_BGK) || pair;
   // FP32 D3Q27 KBC: the compute-heavy sphere-channel step, also with diagnostics
   const bool kbc32 = sk == SK_F32 && coll == XLBG_KBC && d->lattice == XLBG_D3Q27;
   if (!(h16 && !diag) && !kbc32) return 1;
   const int q = d->lattice == XLBG_D2Q9 ? 9 : (d->lattice == XLBG_D3Q19 ? 19 : 27);
   const int eb = kbc32 ? 4 : 2;
-  // rows of 16-byte multiples, at most 992 (16-bit) / 512 (FP32) cells
-  if (a.n2 < 8 || a.n2 > (kbc32 ? 512 : 992) || (a.n2 * eb) % 16 != 0) return 1;
+  const bool seg = pair && !diag;
+  // rows of 16-byte multiples; whole rows of at most 992 (16-bit) / 512 (FP32) cells
+  if (a.n2 < 8 || (a.n2 * eb) % 16 != 0) return 1;
+  if (!seg && a.n2 > (kbc32 ? 512 : 992)) return 1;
   if (a.ncell >= 0x7fffffffLL) return 1;
   if (reinterpret_cast<uintptr_t>(a.f0) % 16 != 0) return 1;
   // the two-cell kernel of collision codes 3 and 4 loads ids and stores outputs in pairs
-  if ((coll == XLBG_BGK_SHIFTED || coll == XLBG_BGK_SHIFTED_SR) &&
-      (reinterpret_cast<uintptr_t>(a.bc_mask) % 2 != 0 || reinterpret_cast<uintptr_t>(a.f1) % 4 != 0))
+  if (pair && (reinterpret_cast<uintptr_t>(a.bc_mask) % 2 != 0 || reinterpret_cast<uintptr_t>(a.f1) % 4 != 0))
     return 1;
-  EncodeTiledFn enc = encode_fn();
   int* err = fault_ptr();
-  if (!enc || !err) return 1;
+  if (!err) return 1;
+
+  if (seg) {
+    // segments: rows of axis 1 per block for about sixteen resident waves of
+    // four blocks a SM over 152 SMs
+    const int nseg = (a.n2 + kSeg - 1) / kSeg;
+    const long long target = 152LL * 4 * 16;
+    long long rows = ((long long)a.n0 * nseg * a.n1 + target - 1) / target;
+    if (rows < 1) rows = 1;
+    if (rows > a.n1) rows = a.n1;
+    const long long bands = (a.n1 + rows - 1) / rows;
+    rows = (a.n1 + bands - 1) / bands;  // even bands
+    int r;
+    if (d->lattice == XLBG_D2Q9)
+      r = launch_step_seg_d2q9(a, sk, coll, fullbc, nseg, (int)rows, err, s);
+    else if (d->lattice == XLBG_D3Q19)
+      r = launch_step_seg_d3q19(a, sk, coll, fullbc, nseg, (int)rows, err, s);
+    else
+      r = launch_step_seg_d3q27(a, sk, coll, fullbc, nseg, (int)rows, err, s);
+    if (r < 0) return 1;
+    if (r) return fail(XLBG_ERR_CUDA, "segmented step kernel launch: %s", cudaGetErrorString((cudaError_t)r));
+    return XLBG_OK;
+  }
+
+  EncodeTiledFn enc = encode_fn();
+  if (!enc) return 1;
 
   const int box = a.n2 < kTmaBox ? a.n2 : kTmaBox;
   CUtensorMap map;
