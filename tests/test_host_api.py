@@ -140,3 +140,31 @@ def test_stepper_rejects_kbc_d3q19(d3q19_fp32):
         IncompressibleNavierStokesStepper(grid_factory((4, 4, 4), device="cpu"), [], collision_type="KBC")
     with pytest.raises(ValueError):
         IncompressibleNavierStokesStepper(grid_factory((4, 4, 4), device="cpu"), [], streaming_scheme="push")
+
+
+@pytest.mark.gpu
+def test_stepper_checks_each_argument_position(d3q19_fp32):
+    """The stepper skips its field checks for tensors it has already accepted in
+    the same argument position; a tensor accepted as f_0 is still rejected as
+    bc_mask, and a reshaped or re-pointed tensor is checked again."""
+    import torch
+
+    from xlb_gb300.operator.stepper import IncompressibleNavierStokesStepper
+
+    grid = grid_factory((12, 10, 8))
+    st = IncompressibleNavierStokesStepper(grid, [], collision_type="BGK")
+    f_0, f_1, bc_mask, missing_mask = st.prepare_fields()
+    for i in range(3):
+        f_0, f_1 = st(f_0, f_1, bc_mask, missing_mask, 1.6, i)
+        f_0, f_1 = f_1, f_0
+    with pytest.raises((TypeError, ValueError)):
+        st(f_0, f_1, f_0, missing_mask, 1.6, 3)
+    with pytest.raises((TypeError, ValueError)):
+        st(f_0, f_1, bc_mask, f_1, 1.6, 3)
+    with pytest.raises(ValueError):
+        st(f_0, f_1, bc_mask, missing_mask.view(missing_mask.shape[0], -1), 1.6, 3)
+    small = torch.empty((f_1.shape[0], 2, 10, 8), dtype=f_1.dtype, device=f_1.device)
+    f_1.set_(small)
+    with pytest.raises(ValueError):
+        st(f_0, f_1, bc_mask, missing_mask, 1.6, 3)
+    torch.cuda.synchronize()

@@ -176,7 +176,7 @@ TMA_CASES = [
     ("D3Q19", (10, 8, 16), "channel_zouhe"),
     ("D3Q19", (10, 8, 16), "channel_regularized"),
     ("D3Q19", (6, 5, 264), "cavity_fullway"),  # two tensor copies per row, the second partly outside
-    ("D3Q19", (4, 3, 520), "periodic"),  # shifted stores: three segments; raw FP16: 1024-thread blocks
+    ("D3Q19", (4, 3, 520), "periodic"),  # shifted stores: three segments; raw FP16: marching kernel
     ("D2Q9", (30, 24), "channel_regularized"),
     ("D3Q27", (10, 8, 16), "channel_pressure"),
     ("D3Q27", (6, 5, 256), "cavity_halfway"),

@@ -1,4 +1,8 @@
-// Fused step with TMA row staging, for the 16-bit stores.
+// Fused step with TMA row staging, one cell per consumer thread: raw FP16
+// stores with XLB-order BGK, and FP32 D3Q27 KBC (plain and with the fused
+// diagnostics).  The shifted 16-bit stores use the segmented two-cell kernel of
+// step_tma_seg.cuh, which shares the ring, the producer hand-off and the
+// bounded waits defined here.
 //
 // The marching kernel keeps each warp's next 19 loads behind its current
 // collision, so with 16-bit populations (half the bytes per cell of FP32) it
@@ -11,7 +15,7 @@
 //         that issues the copies.
 //   stage = for each direction l, the full source row (i0 - c0_l, i1 - c1_l) of
 //         plane l, both wrapped as the stream wraps (stream.py:64-82): Q rows of
-//         PITCH 16-bit values.  The contiguous-axis shift and its wrap are a
+//         PITCH store values.  The contiguous-axis shift and its wrap are a
 //         shared-memory index: thread i2 reads element (i2 - c2_l) mod n2.
 //   ring  = S stages; stage s holds row k while rows k+1 .. k+S-1 are in flight.
 //
@@ -103,11 +107,10 @@ __host__ __device__ constexpr int tma_stages() {
   return L::Q <= 19 ? 5 : 3;
 }
 
-// Consumer threads of a block: one per staged element, at most 992 so that the
-// producer warp fits in a 1024-thread block.
+// Consumer threads of a block: one per staged element (PITCH <= 512).
 template <int PITCH>
 __host__ __device__ constexpr int tma_consumers() {
-  return PITCH > 992 ? 992 : PITCH;
+  return PITCH;
 }
 
 // CTAs per SM the launch bounds ask for (consumers + one producer warp): 16-bit
@@ -116,7 +119,7 @@ __host__ __device__ constexpr int tma_consumers() {
 // spills, while its ~128 registers still fit two 224-thread CTAs (PITCH 192).
 template <int EB, int PITCH>
 __host__ __device__ constexpr int tma_min_blocks() {
-  return EB == 2 ? (PITCH <= 256 ? 4 : (PITCH == 512 ? 2 : 1)) : 1;
+  return EB == 2 ? (PITCH <= 256 ? 4 : 2) : 1;
 }
 
 // shared memory: S stages of Q rows of EB-byte elements, then S "full" and S "empty" mbarriers
@@ -178,7 +181,7 @@ __device__ __forceinline__ void tma_produce(const CUtensorMap& map, unsigned bas
 // has left).  Plane offsets: the fluid path stores through the cell's slot in
 // plane 0 plus 64-bit plane offsets at any size; the boundary paths index
 // f0 / f1 planes with Idx, 32-bit unsigned when Q * cells < 2^32 and 64-bit
-// (WIDE) above, e.g. for 1024 x 1024 x 768 cells.
+// (WIDE) above.
 //
 // Hand-off per stage s (row k, use u = k / S):
 //   producer: wait empty[s] phase u - 1 (u > 0); lane 0 posts expect_tx on
@@ -334,12 +337,12 @@ int launch_tma_pitch(const CUtensorMap& map, const StepArgs& a, bool fullbc, int
                 : launch_tma_variant<L, SK, COLL, PITCH, false, WITH_DIAG>(map, a, fullbc, rows, box, err, s);
 }
 
-// Staged-row width for a contiguous axis of n2 cells.  16-bit stores: 256, 512
-// or 1024 (992 consumers); 4-byte stores: 192, 256 or 512 (n2 <= 512).
+// Staged-row width for a contiguous axis of n2 <= 512 cells: 16-bit stores 256
+// or 512, 4-byte stores 192, 256 or 512.
 template <int EB>
 inline int tma_pitch_for(int n2) {
   if (EB == 4) return n2 <= 192 ? 192 : (n2 <= 256 ? 256 : 512);
-  return n2 <= 256 ? 256 : (n2 <= 512 ? 512 : 1024);
+  return n2 <= 256 ? 256 : 512;
 }
 
 template <int LAT, int SK, int COLL, bool WITH_DIAG = false>
@@ -354,8 +357,7 @@ int launch_tma_t(const CUtensorMap& map, const StepArgs& a, bool fullbc, int row
     return launch_tma_pitch<L, SK, COLL, 512, WITH_DIAG>(map, a, fullbc, rows, box, err, s);
   } else {
     if (pitch == 256) return launch_tma_pitch<L, SK, COLL, 256, WITH_DIAG>(map, a, fullbc, rows, box, err, s);
-    if (pitch == 512) return launch_tma_pitch<L, SK, COLL, 512, WITH_DIAG>(map, a, fullbc, rows, box, err, s);
-    return launch_tma_pitch<L, SK, COLL, 1024, WITH_DIAG>(map, a, fullbc, rows, box, err, s);
+    return launch_tma_pitch<L, SK, COLL, 512, WITH_DIAG>(map, a, fullbc, rows, box, err, s);
   }
 }
 

@@ -61,9 +61,8 @@ int* fault_ptr() {
 // compute, no diagnostics, a contiguous axis of at least 8 cells that is a
 // multiple of 8, fewer than 2^31 cells and a 16-byte aligned f0.  The shifted
 // stores with BGK on their deviations (codes 3 and 4) take the segmented
-// two-cell kernel (any row length); raw FP16 with XLB-order BGK stages whole
-// rows of at most 992 cells, and FP32 D3Q27 KBC (also with diagnostics) whole
-// rows of at most 512.  Boundary paths index planes in 32 bits when Q * cells <
+// two-cell kernel (any row length); raw FP16 with XLB-order BGK and FP32 D3Q27
+// KBC (also with diagnostics) stage whole rows of at most 512 cells.  Boundary paths index planes in 32 bits when Q * cells <
 // 2^32, else in 64 bits (as do the calls made with a.wide set).  Returns 1 when
 // it does not apply (the caller uses the marching kernel), else the status.
 int try_launch_tma(const xlbg_desc* d, const StepArgs& a, bool fullbc, bool diag, cudaStream_t s) {
@@ -78,9 +77,11 @@ int try_launch_tma(const xlbg_desc* d, const StepArgs& a, bool fullbc, bool diag
   const int q = d->lattice == XLBG_D2Q9 ? 9 : (d->lattice == XLBG_D3Q19 ? 19 : 27);
   const int eb = kbc32 ? 4 : 2;
   const bool seg = pair && !diag;
-  // rows of 16-byte multiples; whole rows of at most 992 (16-bit) / 512 (FP32) cells
+  // rows of 16-byte multiples; whole rows of at most 512 cells (a 1024-cell stage
+  // leaves one CTA a SM: raw FP16 at 1024 x 1024 x 768 ran at 36 GLUPS there
+  // against 41 on the marching kernel)
   if (a.n2 < 8 || (a.n2 * eb) % 16 != 0) return 1;
-  if (!seg && a.n2 > (kbc32 ? 512 : 992)) return 1;
+  if (!seg && a.n2 > 512) return 1;
   if (a.ncell >= 0x7fffffffLL) return 1;
   if (reinterpret_cast<uintptr_t>(a.f0) % 16 != 0) return 1;
   // the two-cell kernel of collision codes 3 and 4 loads ids and stores outputs in pairs

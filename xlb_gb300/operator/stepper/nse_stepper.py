@@ -96,6 +96,8 @@ class IncompressibleNavierStokesStepper(Stepper):
         self._cache_key = None
         self._cache = None
         self._diag_slots = None
+        # (argument position, id) -> (weak reference, data pointer, shape, strides) of tensors that passed _check
+        self._checked = {}
 
     # ------------------------------------------------------------------ set-up
 
@@ -150,6 +152,25 @@ class IncompressibleNavierStokesStepper(Stepper):
     # ------------------------------------------------------------------ checks
 
     def _check(self, f_0, f_1, bc_mask, missing_mask):
+        """Type, device, shape, dtype and layout of the four fields.  A tensor
+        that passed once is not checked again while it is the same object with
+        the same storage pointer, shape and strides in the same argument position
+        (dtype and device cannot change in place), so the caller's swap loop
+        pays four lookups a step."""
+        seen = self._checked
+        for role, t in enumerate((f_0, f_1, bc_mask, missing_mask)):
+            e = seen.get((role, id(t)))
+            if e is None or e[0]() is not t or e[1] != t.data_ptr() or e[2] != t.shape or e[3] != t.stride():
+                break
+        else:
+            return
+        self._check_full(f_0, f_1, bc_mask, missing_mask)
+        if len(seen) > 64:
+            seen.clear()
+        for role, t in enumerate((f_0, f_1, bc_mask, missing_mask)):
+            seen[(role, id(t))] = (weakref.ref(t), t.data_ptr(), t.shape, t.stride())
+
+    def _check_full(self, f_0, f_1, bc_mask, missing_mask):
         q = self.velocity_set.q
         fshape = (q,) + tuple(self.grid.field_shape)
         sdt = self.precision_policy.store_precision.torch_dtype
