@@ -136,47 +136,77 @@ def timed_device(stepper, fields, omega, steps, warmup):
     return start.elapsed_time(end), (f_0, f_1, bcm, mm)
 
 
-def timed_e2e(stepper, fields, omega, steps):
-    """The job through the public API with host buffers: H2D of the initial
-    populations and masks from pinned host memory, f_1 made on the device as a
-    copy of f_0 (as prepare_fields makes it, nse_stepper.py:58-98), K per-step
-    ``stepper(...)`` calls with the caller-side swap, D2H of the final
-    populations into a pinned result buffer.
-
-    The result buffer is not the input buffer: on a GB300 with a Grace host a
-    10.2 GB D2H into the pinned pages that the job's H2D had read ran at 16-20
-    GB/s (523-621 ms), into other pinned pages at about 180 GB/s (57 ms).  Both
-    host buffers are allocated and written once before the timed region."""
+def warm_host_buffers(uploads, downloads):
+    """Two untimed passes of each (device, host) upload and (host, device)
+    download, so that the timed copies run at the host link's steady rate.  On
+    the GB300's Grace host the first DMA over freshly pinned pages ran at 15-40
+    GB/s, later ones at 190-210 GB/s; a job that reuses its staging buffers sees
+    the latter.  The device-side contents are rewritten inside the timed region."""
     import torch
 
+    for _ in range(2):
+        for d, h in uploads:
+            d.copy_(h, non_blocking=True)
+        for h, d in downloads:
+            h.copy_(d, non_blocking=True)
+    torch.cuda.synchronize()
+
+
+def timed_e2e(stepper, fields, omega, steps):
+    """The job through the public API with host buffers, as an XLB script runs
+    it: the initial macroscopic state (rho, u) and the two masks H2D from pinned
+    host memory; f_0 = feq(rho, u) (``QuadraticEquilibrium``, what
+    ``initialize_eq`` does) and f_1 a device copy of it (as prepare_fields makes
+    it, nse_stepper.py:58-98); K per-step ``stepper(...)`` calls with the
+    caller-side swap; the macroscopic read-out of the final populations
+    (``Macroscopic``, macroscopic.py:39-66) D2H into pinned result buffers.
+    Host buffers are allocated, written and warmed before the timed region."""
+    import torch
+
+    from xlb_gb300.operator.equilibrium import QuadraticEquilibrium
+    from xlb_gb300.operator.macroscopic import Macroscopic
+
     f_0, f_1, bcm, mm = fields
-    h_in = torch.empty(f_0.shape, dtype=f_0.dtype, pin_memory=True)
-    h_in.copy_(f_0)
-    try:
-        h_out = torch.empty(f_0.shape, dtype=f_0.dtype, pin_memory=True)
-        h_out.copy_(f_0)
-        timed_e2e.result_buffer = "separate pinned buffer"
-    except RuntimeError:  # host memory for a second pinned buffer not available
-        h_out = h_in
-        timed_e2e.result_buffer = "the pinned input buffer (a second one could not be allocated)"
+    vs, pp = stepper.velocity_set, stepper.precision_policy
+    eq, macro = QuadraticEquilibrium(vs, pp), Macroscopic(vs, pp)
+    cdt = pp.compute_precision.torch_dtype
+    spatial = tuple(f_0.shape[1:])
+    rho = torch.ones((1,) + spatial, dtype=cdt, device=f_0.device)
+    u = torch.zeros((vs.d,) + spatial, dtype=cdt, device=f_0.device)
+    # the cavity starts at rest: rho = 1, u = 0
+    h_rho = torch.ones(rho.shape, dtype=cdt).pin_memory()
+    h_u = torch.zeros(u.shape, dtype=cdt).pin_memory()
+    h_rho_out = torch.zeros(rho.shape, dtype=cdt).pin_memory()
+    h_u_out = torch.zeros(u.shape, dtype=cdt).pin_memory()
     hb = bcm.cpu().pin_memory()
     hm = mm.cpu().pin_memory()
-    torch.cuda.synchronize()
+    warm_host_buffers([(rho, h_rho), (u, h_u), (bcm, hb), (mm, hm)], [(h_rho_out, rho), (h_u_out, u)])
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
     barrier()
     t0 = time.perf_counter()
-    f_0.copy_(h_in, non_blocking=True)
-    f_1.copy_(f_0)
+    ev[0].record()
+    rho.copy_(h_rho, non_blocking=True)
+    u.copy_(h_u, non_blocking=True)
     bcm.copy_(hb, non_blocking=True)
     mm.copy_(hm, non_blocking=True)
+    ev[1].record()
+    eq(rho, u, f_0)
+    f_1.copy_(f_0)
+    ev[2].record()
     for i in range(steps):
         f_0, f_1 = stepper(f_0, f_1, bcm, mm, omega, i)
         f_0, f_1 = f_1, f_0
-    h_out.copy_(f_0, non_blocking=True)
+    ev[3].record()
+    macro(f_0, rho, u)
+    h_rho_out.copy_(rho, non_blocking=True)
+    h_u_out.copy_(u, non_blocking=True)
+    ev[4].record()
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
-    h2d = h_in.numel() * h_in.element_size() + hb.numel() + hm.numel()
-    d2h = h_out.numel() * h_out.element_size()
-    return dt, h2d, d2h
+    timed_e2e.phases_ms = {name: ev[k].elapsed_time(ev[k + 1])
+                           for k, name in enumerate(("h2d", "init", "steps", "readout_d2h"))}
+    state = h_rho.numel() * h_rho.element_size() + h_u.numel() * h_u.element_size()
+    return dt, state + hb.numel() + hm.numel(), state
 
 
 _dist = None
@@ -322,27 +352,47 @@ def run_sharded(args, world, rank, local):
         "clocks": clk.summary(),
     }
     if not args.no_e2e:
-        # end to end per rank: its slab's populations and masks H2D, K steps, f_0 D2H
+        # end to end per rank, as the single-GPU leg: the slab's initial rho, u and
+        # masks H2D, f_0 = feq(rho, u), K sharded steps, the read-out of the slab's
+        # own planes D2H
+        from xlb_gb300.operator.equilibrium import QuadraticEquilibrium
+        from xlb_gb300.operator.macroscopic import Macroscopic
+
         (s,) = slabs
-        h_in = s.f_0.cpu().pin_memory()
-        h_out = torch.empty_like(h_in).pin_memory()
+        vs, pp = st.velocity_set, st.precision_policy
+        eq, macro = QuadraticEquilibrium(vs, pp), Macroscopic(vs, pp)
+        spatial = tuple(s.f_0.shape[1:])
+        rho = torch.ones((1,) + spatial, dtype=torch.float32, device=s.f_0.device)
+        u = torch.zeros((vs.d,) + spatial, dtype=torch.float32, device=s.f_0.device)
+        h_rho = torch.ones(rho.shape, dtype=torch.float32).pin_memory()
+        h_u = torch.zeros(u.shape, dtype=torch.float32).pin_memory()
+        h_rho_out = torch.zeros((1, s.t) + spatial[1:], dtype=torch.float32).pin_memory()
+        h_u_out = torch.zeros((vs.d, s.t) + spatial[1:], dtype=torch.float32).pin_memory()
         hb = s.bc_mask.cpu().pin_memory()
         hm = s.missing_mask.cpu().pin_memory()
+        warm_host_buffers([(rho, h_rho), (u, h_u), (s.bc_mask, hb), (s.missing_mask, hm)],
+                          [(h_rho_out, rho[:, 1:s.t + 1]), (h_u_out, u[:, 1:s.t + 1])])
         torch.cuda.synchronize()
         barrier()
         t0 = time.perf_counter()
-        s.f_0.copy_(h_in, non_blocking=True)
-        s.f_1.copy_(s.f_0)
+        rho.copy_(h_rho, non_blocking=True)
+        u.copy_(h_u, non_blocking=True)
         s.bc_mask.copy_(hb, non_blocking=True)
         s.missing_mask.copy_(hm, non_blocking=True)
+        eq(rho, u, s.f_0)
+        s.f_1.copy_(s.f_0)
         ds.run(slabs, 1.8, args.steps)
-        h_out.copy_(s.f_0, non_blocking=True)
+        macro(s.f_0, rho, u)
+        h_rho_out.copy_(rho[:, 1:s.t + 1], non_blocking=True)
+        h_u_out.copy_(u[:, 1:s.t + 1], non_blocking=True)
         torch.cuda.synchronize()
         dt = max_over_ranks(time.perf_counter() - t0)
+        h2d = (h_rho.numel() + h_u.numel()) * 4 + hb.numel() + hm.numel()
+        d2h = (h_rho_out.numel() + h_u_out.numel()) * 4
         out["e2e"] = {"value": world * cells * args.steps / dt / 1e6, "unit": "MLUPS",
-                      "h2d_bytes_per_step": (h_in.numel() * h_in.element_size() + hb.numel() + hm.numel()) / args.steps,
-                      "d2h_bytes_per_step": h_out.numel() * h_out.element_size() / args.steps,
-                      "what": "per rank: slab populations and masks H2D from pinned host, K sharded steps, slab f_0 D2H"}
+                      "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
+                      "what": "per rank: the slab's initial rho, u and masks H2D from pinned host, f_0 = feq(rho, u), "
+                              "K sharded steps, Macroscopic read-out of the slab's planes D2H"}
     if rank == 0:
         print(json.dumps(out))
 
@@ -474,8 +524,8 @@ def main():
             "unit": "MLUPS",
             "h2d_bytes_per_step": h2d / args.steps,
             "d2h_bytes_per_step": d2h / args.steps,
-            "what": "public stepper(...) call per step with caller swap; initial populations and masks H2D from pinned host (f_1 = device copy of f_0, as prepare_fields makes it) and final populations D2H into a pinned result buffer, inside the timed region",
-            "result_buffer": getattr(timed_e2e, "result_buffer", None),
+            "what": "inside the timed region: initial rho, u and the two masks H2D from pinned host; f_0 = feq(rho, u), f_1 = its copy; public stepper(...) call per step with caller swap; Macroscopic read-out of the final state D2H into pinned host",
+            "phases_ms": getattr(timed_e2e, "phases_ms", None),
         }
     if not args.no_adjoint and rank == 0:
         # differentiation: D3Q19 128^3 channel, T=500, checkpoints every 100
