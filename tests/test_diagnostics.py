@@ -12,7 +12,7 @@ from _scenarios import Scenario
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("policy", ["fp32", "fp64", "bf16s"])
+@pytest.mark.parametrize("policy", ["fp32", "fp64", "bf16s", "f16s", "f16sr", "bf16sr"])
 @pytest.mark.parametrize(
     "lattice,shape,layout,collision,force_idx",
     [
@@ -22,10 +22,17 @@ from _scenarios import Scenario
         ("D3Q19", (12, 10, 9), "cavity_halfway", "BGK", 1),
         # FP32 D3Q27 KBC on a contiguous axis of 16: the TMA-staged diagnostics step
         ("D3Q27", (16, 10, 16), "channel_regularized", "KBC", 3),
+        # shifted 16-bit stores on contiguous axes of multiples of 8: the segmented
+        # kernel's diagnostics step (one segment; segments of 256 and 8)
+        ("D3Q19", (16, 10, 16), "channel_zouhe", "BGK", 3),
+        ("D3Q19", (6, 5, 264), "cavity_halfway", "BGK", 1),
     ],
 )
 def test_diagnostics_match_oracle(lattice, shape, layout, collision, force_idx, policy):
     import torch
+
+    if collision == "KBC" and policy.endswith("sr"):
+        pytest.skip("stochastic rounding is a store of BGK on deviations")
 
     sc = Scenario(lattice, shape, layout, policy=policy, collision=collision)
     sc.randomize(seed=31)
@@ -36,7 +43,8 @@ def test_diagnostics_match_oracle(lattice, shape, layout, collision, force_idx, 
         # oracle: force on the input state, mass of the output state
         want_force = O.momentum_transfer(sc.lat, sc.store, f0_np, sc.bc_mask, sc.missing, force_bc.id, sc.T)
         with np.errstate(all="ignore"):
-            n0, n1 = O.step(sc.lat, sc.store, f0_np, f1_np, sc.bc_mask, sc.missing, sc.omega, sc.obcs, sc.collision, sc.T)
+            n0, n1 = O.step(sc.lat, sc.store, f0_np, f1_np, sc.bc_mask, sc.missing, sc.omega, sc.obcs, sc.collision, sc.T,
+                            timestep=t)
         want_mass = O.total_mass(sc.lat, sc.store, n1, sc.bc_mask, sc.T)
         f_0, f_1, out = sc.stepper.step_with_diagnostics(f_0, f_1, bcm, mm, sc.omega, t, force_bc=force_bc)
         got = out.cpu().numpy()

@@ -162,13 +162,28 @@ __device__ __forceinline__ uint32_t pack_rn2(f2 x) {
   return d;
 }
 
+// Mass of the two cells of a stored 32-bit pair word p of direction l, decoded
+// as the one-cell store decodes it and summed in FP32 in direction order (the
+// diagnostics step's per-cell mass).
+template <class L, int SK>
+__device__ __forceinline__ void stored_mass2(uint32_t p, int l, float& m0, float& m1) {
+  using St = Store<SK, float>;
+  using Bits = typename St::Bits;
+  const float v0 = St::dec((Bits)(p & 0xffffu), float(weight<L>(l)));
+  const float v1 = St::dec((Bits)(p >> 16), float(weight<L>(l)));
+  m0 = l == 0 ? v0 : m0 + v0;
+  m1 = l == 0 ? v1 : m1 + v1;
+}
+
 // Collision and store of two neighbouring cells of a row (plane i0, row y,
 // contiguous-axis index z and z + 1, flat index cell and cell + 1; cell even)
 // from their pulled deviations g (low half: cell, high half: cell + 1), as the
 // segmented kernel does it: warps whose 64 cells are all fluid take the packed
-// collision and one 32-bit store per direction; any other warp runs cell_update
-// on its two cells one after the other (boundary cells, skip cells, row ends).
-template <class L, int SK, int COLL, bool FULLBC, bool WIDE>
+// collision and one 32-bit store per direction; any other warp runs
+// cell_update on its two cells one after the other (boundary cells, skip cells,
+// row ends).  DIAG (the diagnostics step) adds each cell's stored mass to dm
+// and, through cell_update, the force on the input to df.
+template <class L, int SK, int COLL, bool FULLBC, bool WIDE, bool DIAG = false>
 __device__ __forceinline__ void pair_finish(const StepArgs& a, f2 (&g)[L::Q], uint16_t ids, int i0, int y, int z,
                                             unsigned cell, double& dm, double (&df)[3]) {
   using T = float;
@@ -178,6 +193,7 @@ __device__ __forceinline__ void pair_finish(const StepArgs& a, f2 (&g)[L::Q], ui
   const size_t plane = (size_t)a.ncell;
   if (__all_sync(0xffffffffu, ids == 0)) {
     bgk_shifted2<L, SK>(g, omega_of<T>(a));
+    float m0 = 0.0f, m1 = 0.0f;
     if constexpr (COLL == 4) {
       // the one-cell store rounds (cell c, direction l) with the low (l even) or
       // high (l odd) 16 bits of sr_bits(sr_seed(c, t), l / 2): assemble those
@@ -188,14 +204,22 @@ __device__ __forceinline__ void pair_finish(const StepArgs& a, f2 (&g)[L::Q], ui
         const uint32_t w0 = sr_bits(s0, l / 2), w1 = sr_bits(s1, l / 2);
         const uint32_t rb = (l & 1) ? __byte_perm(w0, w1, 0x7632) : __byte_perm(w0, w1, 0x5410);
         uint32_t* __restrict__ dst = reinterpret_cast<uint32_t*>(static_cast<Bits*>(a.f1) + (size_t)l * plane + cell);
-        *dst = sr_pack<SK>(lo2(g[l]), hi2(g[l]), rb);
+        const uint32_t p = sr_pack<SK>(lo2(g[l]), hi2(g[l]), rb);
+        *dst = p;
+        if constexpr (DIAG) stored_mass2<L, SK>(p, l, m0, m1);
       }
     } else {
 #pragma unroll
       for (int l = 0; l < Q; ++l) {
         uint32_t* __restrict__ dst = reinterpret_cast<uint32_t*>(static_cast<Bits*>(a.f1) + (size_t)l * plane + cell);
-        *dst = pack_rn2<SK>(g[l]);
+        const uint32_t p = pack_rn2<SK>(g[l]);
+        *dst = p;
+        if constexpr (DIAG) stored_mass2<L, SK>(p, l, m0, m1);
       }
+    }
+    if constexpr (DIAG) {
+      dm += (double)m0;
+      dm += (double)m1;
     }
   } else {
 #pragma unroll
@@ -205,7 +229,16 @@ __device__ __forceinline__ void pair_finish(const StepArgs& a, f2 (&g)[L::Q], ui
         T f[Q];
 #pragma unroll
         for (int l = 0; l < Q; ++l) f[l] = h == 0 ? lo2(g[l]) : hi2(g[l]);
-        cell_update<L, SK, T, COLL, FULLBC, false>(a, i0, y, z + h, (Idx)(cell + (unsigned)h), id, f, dm, df);
+        if constexpr (DIAG) {
+          double dmc = 0.0, dfc[3] = {0.0, 0.0, 0.0};
+          cell_update<L, SK, T, COLL, FULLBC, true>(a, i0, y, z + h, (Idx)(cell + (unsigned)h), id, f, dmc, dfc);
+          dm += dmc;
+          df[0] += dfc[0];
+          df[1] += dfc[1];
+          df[2] += dfc[2];
+        } else {
+          cell_update<L, SK, T, COLL, FULLBC, false>(a, i0, y, z + h, (Idx)(cell + (unsigned)h), id, f, dm, df);
+        }
       }
     }
   }

@@ -3,8 +3,8 @@
 #include "step_tma_seg.cuh"
 
 namespace xlbg {
-int launch_step_seg_d3q19(const StepArgs& a, int sk, int coll, bool fullbc, int nseg, int rows, int* err,
+int launch_step_seg_d3q19(const StepArgs& a, int sk, int coll, bool fullbc, bool diag, int nseg, int rows, int* err,
                          cudaStream_t s) {
-  return launch_seg_lattice<1>(a, sk, coll, fullbc, nseg, rows, err, s);
+  return launch_seg_lattice<1>(a, sk, coll, fullbc, diag, nseg, rows, err, s);
 }
 }  // namespace xlbg

@@ -380,11 +380,11 @@ int launch_step_tma_d3q27(const CUtensorMap& map, const StepArgs& a, int sk, int
 // Segmented two-cell kernel (step_tma_seg.cuh): shifted 16-bit stores, codes 3
 // and 4; blocks own kSeg cells of the contiguous axis.
 constexpr int kSeg = 256;
-int launch_step_seg_d2q9(const StepArgs& a, int sk, int coll, bool fullbc, int nseg, int rows, int* err,
+int launch_step_seg_d2q9(const StepArgs& a, int sk, int coll, bool fullbc, bool diag, int nseg, int rows, int* err,
                          cudaStream_t s);
-int launch_step_seg_d3q19(const StepArgs& a, int sk, int coll, bool fullbc, int nseg, int rows, int* err,
+int launch_step_seg_d3q19(const StepArgs& a, int sk, int coll, bool fullbc, bool diag, int nseg, int rows, int* err,
                           cudaStream_t s);
-int launch_step_seg_d3q27(const StepArgs& a, int sk, int coll, bool fullbc, int nseg, int rows, int* err,
+int launch_step_seg_d3q27(const StepArgs& a, int sk, int coll, bool fullbc, bool diag, int nseg, int rows, int* err,
                           cudaStream_t s);
 // FP32 store, KBC, D3Q27, with the diagnostics step (step_tma_d3q27_kbc.cu).
 int launch_step_tma_d3q27_kbc32(const CUtensorMap& map, const StepArgs& a, bool fullbc, int rows, int box, int* err,

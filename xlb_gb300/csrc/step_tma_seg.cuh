@@ -118,9 +118,13 @@ __device__ __forceinline__ void seg_produce(const StepArgs& a, unsigned base, un
 // Grid: (n0 * nseg, ceil(n1 / rows)), block kSegConsumers + 32 threads,
 // seg_smem_bytes<L>() of dynamic shared memory; block x = i0 * nseg + segment.
 // n2 a multiple of 8, cell offsets fit 31 bits, f0 16-byte aligned, bc_mask
-// 2-byte and f1 4-byte aligned (the host checks).
-template <class L, int SK, int COLL, bool FULLBC, bool WIDE>
-__global__ void __launch_bounds__(kSegConsumers + 32, 4)
+// 2-byte and f1 4-byte aligned (the host checks).  DIAG: the diagnostics step
+// (mass of the output as stored, force on the input, as the one-cell kernels
+// define them): per-thread FP64 sums, reduced over each consumer warp by
+// shuffles and added to the slot array by lane 0.
+template <class L, int SK, int COLL, bool FULLBC, bool WIDE, bool DIAG>
+// (three CTAs a SM for DIAG: capped at 96 registers for four, it spilled)
+__global__ void __launch_bounds__(kSegConsumers + 32, DIAG ? 3 : 4)
     step_kernel_seg(const StepArgs a, int nseg, int rows, int* err) {
   using St = Store<SK, float>;
   using Bits = typename St::Bits;
@@ -200,40 +204,58 @@ __global__ void __launch_bounds__(kSegConsumers + 32, 4)
     }
     __syncwarp();
     if (lane == 0) mbar_arrive(empty + 8 * s);
-    pair_finish<L, SK, COLL, FULLBC, WIDE>(a, g, ids, i0, y, z0 + p0, cell, dm, df);
+    pair_finish<L, SK, COLL, FULLBC, WIDE, DIAG>(a, g, ids, i0, y, z0 + p0, cell, dm, df);
+  }
+  if constexpr (DIAG) {
+    double v[4] = {dm, df[0], df[1], df[2]};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+    }
+    if (lane == 0) {
+      const unsigned slot = ((blockIdx.x * gridDim.y + blockIdx.y) * CONSUMER_WARPS + (tid >> 5)) % kDiagSlots;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) atomicAdd(a.diag_slots + slot * 4 + k, v[k]);
+    }
   }
 }
 
-template <class L, int SK, int COLL, bool FULLBC, bool WIDE>
+template <class L, int SK, int COLL, bool FULLBC, bool WIDE, bool DIAG>
 int launch_seg_kernel(const StepArgs& a, int nseg, int rows, int* err, cudaStream_t s) {
   const unsigned smem = seg_smem_bytes<L>();
-  static const bool attr = cudaFuncSetAttribute(step_kernel_seg<L, SK, COLL, FULLBC, WIDE>,
+  static const bool attr = cudaFuncSetAttribute(step_kernel_seg<L, SK, COLL, FULLBC, WIDE, DIAG>,
                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem) == cudaSuccess;
   if (!attr) return (int)cudaErrorInvalidValue;
   const dim3 grid((unsigned)a.n0 * (unsigned)nseg, (unsigned)((a.n1 + rows - 1) / rows));
-  step_kernel_seg<L, SK, COLL, FULLBC, WIDE><<<grid, kSegConsumers + 32, smem, s>>>(a, nseg, rows, err);
+  step_kernel_seg<L, SK, COLL, FULLBC, WIDE, DIAG><<<grid, kSegConsumers + 32, smem, s>>>(a, nseg, rows, err);
   return (int)cudaGetLastError();
 }
 
+// The diagnostics step always runs with the full BC code (the force BC's cells
+// go through it), so DIAG is instantiated with FULLBC only.
 template <int LAT, int SK, int COLL>
-int launch_seg_t(const StepArgs& a, bool fullbc, int nseg, int rows, int* err, cudaStream_t s) {
+int launch_seg_t(const StepArgs& a, bool fullbc, bool diag, int nseg, int rows, int* err, cudaStream_t s) {
   using L = Lattice<LAT>;
+  if (diag)
+    return a.wide ? launch_seg_kernel<L, SK, COLL, true, true, true>(a, nseg, rows, err, s)
+                  : launch_seg_kernel<L, SK, COLL, true, false, true>(a, nseg, rows, err, s);
   if (a.wide)
-    return fullbc ? launch_seg_kernel<L, SK, COLL, true, true>(a, nseg, rows, err, s)
-                  : launch_seg_kernel<L, SK, COLL, false, true>(a, nseg, rows, err, s);
-  return fullbc ? launch_seg_kernel<L, SK, COLL, true, false>(a, nseg, rows, err, s)
-                : launch_seg_kernel<L, SK, COLL, false, false>(a, nseg, rows, err, s);
+    return fullbc ? launch_seg_kernel<L, SK, COLL, true, true, false>(a, nseg, rows, err, s)
+                  : launch_seg_kernel<L, SK, COLL, false, true, false>(a, nseg, rows, err, s);
+  return fullbc ? launch_seg_kernel<L, SK, COLL, true, false, false>(a, nseg, rows, err, s)
+                : launch_seg_kernel<L, SK, COLL, false, false, false>(a, nseg, rows, err, s);
 }
 
-// Per-lattice entry (step_tma_*.cu): shifted FP16 / BF16 with collision code 3
+// Per-lattice entry (step_seg_*.cu): shifted FP16 / BF16 with collision code 3
 // or 4; other combinations return -1.
 template <int LAT>
-int launch_seg_lattice(const StepArgs& a, int sk, int coll, bool fullbc, int nseg, int rows, int* err,
+int launch_seg_lattice(const StepArgs& a, int sk, int coll, bool fullbc, bool diag, int nseg, int rows, int* err,
                        cudaStream_t s) {
-  if (sk == SK_F16S && coll == 3) return launch_seg_t<LAT, SK_F16S, 3>(a, fullbc, nseg, rows, err, s);
-  if (sk == SK_BF16S && coll == 3) return launch_seg_t<LAT, SK_BF16S, 3>(a, fullbc, nseg, rows, err, s);
-  if (sk == SK_F16S && coll == 4) return launch_seg_t<LAT, SK_F16S, 4>(a, fullbc, nseg, rows, err, s);
-  if (sk == SK_BF16S && coll == 4) return launch_seg_t<LAT, SK_BF16S, 4>(a, fullbc, nseg, rows, err, s);
+  if (sk == SK_F16S && coll == 3) return launch_seg_t<LAT, SK_F16S, 3>(a, fullbc, diag, nseg, rows, err, s);
+  if (sk == SK_BF16S && coll == 3) return launch_seg_t<LAT, SK_BF16S, 3>(a, fullbc, diag, nseg, rows, err, s);
+  if (sk == SK_F16S && coll == 4) return launch_seg_t<LAT, SK_F16S, 4>(a, fullbc, diag, nseg, rows, err, s);
+  if (sk == SK_BF16S && coll == 4) return launch_seg_t<LAT, SK_BF16S, 4>(a, fullbc, diag, nseg, rows, err, s);
   return -1;
 }
 

@@ -57,12 +57,12 @@ int* fault_ptr() {
 
 }  // namespace
 
-// Launches the TMA-staged step when it applies: a 16-bit store with FP32
-// compute, no diagnostics, a contiguous axis of at least 8 cells that is a
-// multiple of 8, fewer than 2^31 cells and a 16-byte aligned f0.  The shifted
-// stores with BGK on their deviations (codes 3 and 4) take the segmented
-// two-cell kernel (any row length); raw FP16 with XLB-order BGK and FP32 D3Q27
-// KBC (also with diagnostics) stage whole rows of at most 512 cells.  Boundary paths index planes in 32 bits when Q * cells <
+// Launches the TMA-staged step when it applies: FP32 compute, a contiguous
+// axis of at least 8 cells that is a multiple of 8, fewer than 2^31 cells and a
+// 16-byte aligned f0.  The shifted 16-bit stores with BGK on their deviations
+// (codes 3 and 4) take the segmented two-cell kernel (any row length, also the
+// diagnostics step); raw FP16 with XLB-order BGK (not the diagnostics step) and
+// FP32 D3Q27 KBC (also with diagnostics) stage whole rows of at most 512 cells.  Boundary paths index planes in 32 bits when Q * cells <
 // 2^32, else in 64 bits (as do the calls made with a.wide set).  Returns 1 when
 // it does not apply (the caller uses the marching kernel), else the status.
 int try_launch_tma(const xlbg_desc* d, const StepArgs& a, bool fullbc, bool diag, cudaStream_t s) {
@@ -70,13 +70,13 @@ int try_launch_tma(const xlbg_desc* d, const StepArgs& a, bool fullbc, bool diag
   const int sk = d->store;
   const int coll = d->collision;
   const bool pair = (sk == SK_F16S || sk == SK_BF16S) && (coll == XLBG_BGK_SHIFTED || coll == XLBG_BGK_SHIFTED_SR);
-  const bool h16 = (sk == SK_F16 && coll == XLBG_BGK) || pair;
+  const bool raw16 = sk == SK_F16 && coll == XLBG_BGK;
   // FP32 D3Q27 KBC: the compute-heavy sphere-channel step, also with diagnostics
   const bool kbc32 = sk == SK_F32 && coll == XLBG_KBC && d->lattice == XLBG_D3Q27;
-  if (!(h16 && !diag) && !kbc32) return 1;
+  if (!(pair || (raw16 && !diag) || kbc32)) return 1;
   const int q = d->lattice == XLBG_D2Q9 ? 9 : (d->lattice == XLBG_D3Q19 ? 19 : 27);
   const int eb = kbc32 ? 4 : 2;
-  const bool seg = pair && !diag;
+  const bool seg = pair;
   // rows of 16-byte multiples; whole rows of at most 512 cells (a 1024-cell stage
   // leaves one CTA a SM: raw FP16 at 1024 x 1024 x 768 ran at 36 GLUPS there
   // against 41 on the marching kernel)
@@ -102,11 +102,11 @@ int try_launch_tma(const xlbg_desc* d, const StepArgs& a, bool fullbc, bool diag
     rows = (a.n1 + bands - 1) / bands;  // even bands
     int r;
     if (d->lattice == XLBG_D2Q9)
-      r = launch_step_seg_d2q9(a, sk, coll, fullbc, nseg, (int)rows, err, s);
+      r = launch_step_seg_d2q9(a, sk, coll, fullbc, diag, nseg, (int)rows, err, s);
     else if (d->lattice == XLBG_D3Q19)
-      r = launch_step_seg_d3q19(a, sk, coll, fullbc, nseg, (int)rows, err, s);
+      r = launch_step_seg_d3q19(a, sk, coll, fullbc, diag, nseg, (int)rows, err, s);
     else
-      r = launch_step_seg_d3q27(a, sk, coll, fullbc, nseg, (int)rows, err, s);
+      r = launch_step_seg_d3q27(a, sk, coll, fullbc, diag, nseg, (int)rows, err, s);
     if (r < 0) return 1;
     if (r) return fail(XLBG_ERR_CUDA, "segmented step kernel launch: %s", cudaGetErrorString((cudaError_t)r));
     return XLBG_OK;
