@@ -182,6 +182,62 @@ static void FN(zouhe_like)(const lattice_t* L, T* f, uint32_t miss, T aux, int k
 static inline int FN(wrap)(int i, int n) { return i < 0 ? n - 1 : (i >= n ? 0 : i); }
 
 /*
+ * XLB-order BGK (collision 0) on a chunk of nk <= FLUID_W fluid cells z .. z+nk-1
+ * of one row, 1 <= z and z + nk <= n2 - 1 (no wrap along the contiguous
+ * axis).  Every cell gets exactly the per-cell operations of the generic path
+ * (macroscopic, equilibrium, f - omega (f - feq), in the same order); the loops
+ * run over the chunk's cells innermost so the compiler can vectorise them.
+ * Speed only: results are bit-identical to the per-cell path.
+ */
+#ifndef FLUID_W
+#define FLUID_W 256
+#endif
+static void FN(fluid_chunk)(const lattice_t* L, const T* f0, T* f1, int64_t N, const int64_t* src_row,
+                            int64_t cell0, int z, int nk, T omega) {
+  const int Q = L->q;
+  T F[MAXQ][FLUID_W], R[FLUID_W], U[3][FLUID_W], US[FLUID_W];
+  for (int l = 0; l < Q; ++l) {
+    const T* src = f0 + src_row[l] + z - L->ax[l][2];
+    for (int k = 0; k < nk; ++k) F[l][k] = src[k];
+  }
+  for (int k = 0; k < nk; ++k) R[k] = (T)0 + F[0][k];
+  for (int l = 1; l < Q; ++l)
+    for (int k = 0; k < nk; ++k) R[k] = R[k] + F[l][k];
+  for (int d = 0; d < L->d; ++d) {
+    T acc[FLUID_W];
+    for (int k = 0; k < nk; ++k) acc[k] = (T)0;
+    for (int l = 0; l < Q; ++l) {
+      if (L->c[l][d] == 1)
+        for (int k = 0; k < nk; ++k) acc[k] = acc[k] + F[l][k];
+      if (L->c[l][d] == -1)
+        for (int k = 0; k < nk; ++k) acc[k] = acc[k] - F[l][k];
+    }
+    for (int k = 0; k < nk; ++k) U[d][k] = acc[k] / R[k];
+  }
+  for (int k = 0; k < nk; ++k) US[k] = U[0][k] * U[0][k];
+  for (int d = 1; d < L->d; ++d)
+    for (int k = 0; k < nk; ++k) US[k] = US[k] + U[d][k] * U[d][k];
+  for (int k = 0; k < nk; ++k) US[k] = (T)1.5 * US[k];
+  for (int l = 0; l < Q; ++l) {
+    const T w = (T)L->w[l];
+    T cu[FLUID_W];
+    for (int k = 0; k < nk; ++k) cu[k] = (T)0;
+    for (int d = 0; d < L->d; ++d) {
+      if (L->c[l][d] == 1)
+        for (int k = 0; k < nk; ++k) cu[k] = cu[k] + U[d][k];
+      if (L->c[l][d] == -1)
+        for (int k = 0; k < nk; ++k) cu[k] = cu[k] - U[d][k];
+    }
+    T* dst = f1 + (int64_t)l * N + cell0;
+    for (int k = 0; k < nk; ++k) {
+      const T c3 = cu[k] * (T)3;
+      const T feq = R[k] * w * ((T)1 + c3 * ((T)1 + (T)0.5 * c3) - US[k]);
+      dst[k] = F[l][k] - omega * (F[l][k] - feq);
+    }
+  }
+}
+
+/*
  * One step.  f0 is read (and receives the aux recovery writes afterwards), f1 is
  * written.  Per-BC arrays: ids, kinds, rhos, us (3 per BC).  Returns 0.
  */
@@ -227,8 +283,22 @@ int FN(lbm_ref_step)(int lattice, int collision, int64_t nx, int64_t ny, int64_t
 #pragma omp parallel for schedule(static)
   for (int64_t row = 0; row < (int64_t)n0 * n1; ++row) {
     const int i0 = (int)(row / n1), i1 = (int)(row % n1);
+    int64_t src_row[MAXQ];
+    for (int l = 0; l < Q; ++l)
+      src_row[l] = (int64_t)l * N +
+                   ((int64_t)FN(wrap)(i0 - L->ax[l][0], n0) * n1 + FN(wrap)(i1 - L->ax[l][1], n1)) * n2;
     for (int i2 = 0; i2 < n2; ++i2) {
       const int64_t cell = row * n2 + i2;
+      if (collision == 0 && i2 >= 1 && i2 < n2 - 1) {
+        const int nk = n2 - 1 - i2 < FLUID_W ? n2 - 1 - i2 : FLUID_W;
+        int fluid = 1;
+        for (int k = 0; k < nk; ++k) fluid &= bcm[cell + k] == 0;
+        if (fluid) {
+          FN(fluid_chunk)(L, f0, f1, N, src_row, cell, i2, nk, omega);
+          i2 += nk - 1;
+          continue;
+        }
+      }
       const uint8_t id = bcm[cell];
       if (id == 255) continue;
       T f[MAXQ], fo[MAXQ], feq[MAXQ], u[3], rho;
