@@ -232,3 +232,24 @@ def stream_handle(stream=None):
 
     s = stream if stream is not None else torch.cuda.current_stream()
     return ctypes.c_void_p(s.cuda_stream)
+
+
+def _raw_stream_getter():
+    import torch
+
+    raw = getattr(torch._C, "_cuda_getCurrentRawStream", None)
+    if raw is not None:
+        return raw
+    return lambda device: torch.cuda.current_stream(device).cuda_stream
+
+
+_raw_stream = None
+
+
+def raw_stream(device_index):
+    """cudaStream_t (as an int) of torch's current stream on a device: the
+    per-step calls' cheap form of stream_handle (0.1 us against 3 us)."""
+    global _raw_stream
+    if _raw_stream is None:
+        _raw_stream = _raw_stream_getter()
+    return _raw_stream(device_index)

@@ -96,7 +96,8 @@ class IncompressibleNavierStokesStepper(Stepper):
         self._cache_key = None
         self._cache = None
         self._diag_slots = None
-        # (argument position, id) -> (weak reference, data pointer, shape, strides) of tensors that passed _check
+        # ids of (f_0, f_1, bc_mask, missing_mask) -> (weak reference, data pointer, shape, strides) of each,
+        # for argument tuples that passed _check
         self._checked = {}
 
     # ------------------------------------------------------------------ set-up
@@ -156,19 +157,17 @@ class IncompressibleNavierStokesStepper(Stepper):
         that passed once is not checked again while it is the same object with
         the same storage pointer, shape and strides in the same argument position
         (dtype and device cannot change in place), so the caller's swap loop
-        pays four lookups a step."""
-        seen = self._checked
-        for role, t in enumerate((f_0, f_1, bc_mask, missing_mask)):
-            e = seen.get((role, id(t)))
-            if e is None or e[0]() is not t or e[1] != t.data_ptr() or e[2] != t.shape or e[3] != t.stride():
-                break
-        else:
+        (two argument tuples) pays one lookup a step."""
+        args = (f_0, f_1, bc_mask, missing_mask)
+        key = (id(f_0), id(f_1), id(bc_mask), id(missing_mask))
+        e = self._checked.get(key)
+        if e is not None and all(r() is t and t.data_ptr() == p and t.shape == sh and t.stride() == sd
+                                 for t, (r, p, sh, sd) in zip(args, e)):
             return
         self._check_full(f_0, f_1, bc_mask, missing_mask)
-        if len(seen) > 64:
-            seen.clear()
-        for role, t in enumerate((f_0, f_1, bc_mask, missing_mask)):
-            seen[(role, id(t))] = (weakref.ref(t), t.data_ptr(), t.shape, t.stride())
+        if len(self._checked) > 16:
+            self._checked.clear()
+        self._checked[key] = tuple((weakref.ref(t), t.data_ptr(), t.shape, t.stride()) for t in args)
 
     def _check_full(self, f_0, f_1, bc_mask, missing_mask):
         q = self.velocity_set.q
@@ -231,13 +230,15 @@ class IncompressibleNavierStokesStepper(Stepper):
         self._check(f_0, f_1, bc_mask, missing_mask)
         bits, rec_cells, scratch = self._aux_state(bc_mask, missing_mask)
         rc, nrec, scr = self._rec_args(rec_cells, scratch)
-        _lib.check(
-            self._lib.xlbg_step(
-                self.desc, _lib.ptr(f_0), _lib.ptr(f_1), _lib.ptr(bc_mask), _lib.ptr(bits), rc, nrec, scr,
-                float(omega), int(timestep), _lib.stream_handle(),
-            )
+        rc_ = self._lib.xlbg_step(
+            self.desc, f_0.data_ptr(), f_1.data_ptr(), bc_mask.data_ptr(), bits.data_ptr(), rc, nrec, scr,
+            float(omega), int(timestep), _lib.raw_stream(f_0.get_device()),
         )
+        if rc_:
+            _lib.check(rc_)
         return f_0, f_1
+
+    __call__ = cuda_implementation
 
     def run(self, f_0, f_1, bc_mask, missing_mask, omega, num_steps, timestep0=0):
         """``num_steps`` steps of the swap loop above in one C call.  Returns
@@ -249,7 +250,7 @@ class IncompressibleNavierStokesStepper(Stepper):
         _lib.check(
             self._lib.xlbg_run(
                 self.desc, _lib.ptr(f_0), _lib.ptr(f_1), _lib.ptr(bc_mask), _lib.ptr(bits), rc, nrec, scr,
-                float(omega), int(timestep0), int(num_steps), _lib.stream_handle(),
+                float(omega), int(timestep0), int(num_steps), _lib.raw_stream(f_0.get_device()),
             )
         )
         return (f_1, f_0) if num_steps % 2 else (f_0, f_1)
@@ -270,7 +271,8 @@ class IncompressibleNavierStokesStepper(Stepper):
         _lib.check(
             self._lib.xlbg_step_diag(
                 self.desc, _lib.ptr(f_0), _lib.ptr(f_1), _lib.ptr(bc_mask), _lib.ptr(bits), rc, nrec, scr,
-                float(omega), int(timestep), force_id, _lib.ptr(self._diag_slots), _lib.ptr(out), _lib.stream_handle(),
+                float(omega), int(timestep), force_id, _lib.ptr(self._diag_slots), _lib.ptr(out),
+                _lib.raw_stream(f_0.get_device()),
             )
         )
         return f_0, f_1, out
