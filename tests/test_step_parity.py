@@ -362,3 +362,35 @@ def test_stochastic_rounding_run_uses_the_timesteps():
     b = sc.gpu_steps(4, use_run=True)
     _compare(b[0], a[0], "run f_0")
     _compare(b[1], a[1], "run f_1")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("lattice,shape,layout,policy,collision", [
+    ("D2Q9", (30, 18), "channel_zouhe", "fp32", "BGK"),
+    ("D3Q19", (16, 10, 10), "channel_regularized", "fp32", "BGK"),
+    ("D3Q19", (10, 8, 16), "cavity_fullway", "f16s", "BGK"),
+    ("D3Q27", (10, 8, 16), "channel_regularized", "fp32", "KBC"),
+    ("D3Q19", (12, 10, 9), "cavity_halfway", "fp64", "BGK"),
+])
+def test_run_longer_loops_equal_step_loop(lattice, shape, layout, policy, collision):
+    """xlbg_run over 11 steps (an odd count: the result is in the other buffer)
+    equals the oracle, and 11 more on the same buffers equal 22 per-step calls,
+    bit for bit."""
+    import torch
+
+    sc = Scenario(lattice, shape, layout, policy=policy, collision=collision)
+    sc.randomize(seed=21)
+    want0, want1 = sc.oracle_steps(11)
+    f_0, f_1, bcm, mm = sc.gpu_fields()
+    f_0, f_1 = sc.stepper.run(f_0, f_1, bcm, mm, sc.omega, 11)
+    torch.cuda.synchronize()
+    _compare(sc.to_numpy(f_0), want0, "f_0 after 11")
+    _compare(sc.to_numpy(f_1), want1, "f_1 after 11")
+    f_0, f_1 = sc.stepper.run(f_0, f_1, bcm, mm, sc.omega, 11)
+    g_0, g_1, gbcm, gmm = sc.gpu_fields()
+    for i in range(22):
+        g_0, g_1 = sc.stepper(g_0, g_1, gbcm, gmm, sc.omega, i)
+        g_0, g_1 = g_1, g_0
+    torch.cuda.synchronize()
+    _compare(sc.to_numpy(f_0), sc.to_numpy(g_0), "f_0 after 22")
+    _compare(sc.to_numpy(f_1), sc.to_numpy(g_1), "f_1 after 22")
