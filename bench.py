@@ -400,12 +400,19 @@ def run_sharded(args, world, rank, local):
 
 def run_reference(args):
     """--impl reference: XLB's own CPU path needs warp or jax, neither installable
-    here, so the C restatement of that path runs on this host's cores instead,
-    on the same cavity (n^3, 512^3 by default) as the GPU arm."""
+    here, so the C restatement of that path runs on this host's cores instead:
+    on the GPU arm's cavity (n^3, 512^3 by default) when the W + K steps fit in
+    about two minutes of host time (about 330 MLUPS on 16 Arm cores), else on the
+    largest of 384^3, 256^3, 192^3, 128^3 that does (the JSON line names it)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    total = max(1, args.steps + args.warmup)
     n = args.n
+    for edge in (384, 256, 192, 128):
+        if total * n**3 <= 4e10 or n <= edge:
+            break
+        n = edge
     st, f0, f1, threads = cref_cavity(n)
     f0, f1 = st.run(f0, f1, 1.8, args.warmup)
     t0 = time.perf_counter()
