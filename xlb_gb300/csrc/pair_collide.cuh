@@ -6,8 +6,13 @@
 // the collision as a pair of floats in one 64-bit register, operated on by
 // Blackwell's packed FP32 instructions (fma/add/sub/mul.rn.f32x2).  Each lane of
 // a packed instruction is the scalar instruction of bgk_shifted, in the same
-// order with the same rounding (explicit .rn: no contraction), so the results
-// are bit-identical to the one-cell kernels and the oracle.  The two cells'
+// order with the same rounding, so the results are bit-identical to the one-cell
+// kernels and the oracle.  Unlike scalar .rn arithmetic, a packed mul.rn.f32x2
+// whose only use is a packed add can be contracted by ptxas into a packed FMA
+// (measured: a direction-paired equilibrium written that way differed from the
+// scalar one in 0.4 % of values), so every fused step here is an explicit fma2
+// and no single-use mul2 feeds an add2 / sub2; the parity tests check the bits
+// at every size.  The two cells'
 // values of a direction convert with one cvt.rn.{f16x2,bf16x2} and store as one
 // 32-bit word (the pair is 4-byte aligned: rows hold a multiple of 8 cells).
 // With stochastic rounding (code 4) the conversion is cvt.rs with each half
