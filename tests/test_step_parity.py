@@ -212,6 +212,8 @@ SEG_CASES = [
     ("D2Q9", (12, 528), "cavity_fullway"),
     ("D3Q27", (10, 8, 16), "channel_pressure"),
     ("D3Q27", (4, 3, 768), "cavity_halfway"),
+    ("D3Q19", (6, 5, 8), "periodic"),  # the shortest row: one 8-cell segment, both aprons wrapped
+    ("D3Q27", (5, 4, 24), "channel_regularized"),
 ]
 
 
