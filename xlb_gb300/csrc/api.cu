@@ -314,12 +314,13 @@ int fill_step_args(const xlbg_desc* d, const void* f0, void* f1, const uint8_t* 
 }
 
 // Rows per thread of the marching kernel: at least eight blocks per SM of a
-// 152-SM GB300 and at most 64 rows per thread.
+// 152-SM GB300 and at most 32 rows per thread (D3Q19 FP32 at 512^3: 64 rows
+// 41.2-41.7, 32 rows 41.7, 16 rows 41.8 GLUPS: within run-to-run spread).
 static int choose_chunk(const StepArgs& a, int threads) {
   const long long columns = (long long)a.n0 * ((a.n2 + threads - 1) / threads);
   long long chunk = (long long)a.n1 * columns / (152LL * 8);
   if (chunk < 1) chunk = 1;
-  if (chunk > 64) chunk = 64;
+  if (chunk > 32) chunk = 32;
   return (int)chunk;
 }
 

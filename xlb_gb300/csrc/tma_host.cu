@@ -91,11 +91,14 @@ int try_launch_tma(const xlbg_desc* d, const StepArgs& a, bool fullbc, bool diag
   if (!err) return 1;
 
   if (seg) {
-    // segments: rows of axis 1 per block for about sixteen resident waves of
-    // four blocks a SM over 152 SMs
+    // segments: rows of axis 1 per block for about 32 resident waves of four
+    // blocks a SM over 152 SMs, at most 96 rows (D3Q19 FP16S, rows per block:
+    // 512^3 54 -> 82.6, 27 -> 84.4, 14 -> 83.5 GLUPS; 1024 x 1024 x 768 162 ->
+    // 82.0, 81 -> 83.4; the last wave's imbalance against each block's ring fill)
     const int nseg = (a.n2 + kSeg - 1) / kSeg;
-    const long long target = 152LL * 4 * 16;
+    const long long target = 152LL * 4 * 32;
     long long rows = ((long long)a.n0 * nseg * a.n1 + target - 1) / target;
+    if (rows > 96) rows = 96;
     if (rows < 1) rows = 1;
     if (rows > a.n1) rows = a.n1;
     const long long bands = (a.n1 + rows - 1) / rows;
