@@ -129,10 +129,11 @@ int try_launch_tma(const xlbg_desc* d, const StepArgs& a, bool fullbc, bool diag
           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
     return 1;
 
-  // rows of axis 1 per CTA: about sixteen resident waves of CTAs over 152 SMs
-  // (measured at 512^3: 54 rows 58.2, 108 rows 57.3, 27 rows 57.2 GLUPS)
+  // rows of axis 1 per CTA: about 32 resident waves of CTAs over 152 SMs (FP32
+  // D3Q27 KBC on the 768 x 192 x 192 sphere channel, developed flow: 16 waves
+  // 16.2, 32 waves 16.9, 64 waves 16.8 GLUPS)
   const int cps = eb == 4 ? (a.n2 <= 256 ? 2 : 1) : (a.n2 <= 256 ? 4 : (a.n2 <= 512 ? 2 : 1));
-  const long long target = 152LL * cps * 16;
+  const long long target = 152LL * cps * 32;
   long long rows = ((long long)a.n0 * a.n1 + target - 1) / target;
   if (rows < 1) rows = 1;
   if (rows > a.n1) rows = a.n1;
